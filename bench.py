@@ -1,0 +1,344 @@
+"""Benchmark of the intracule hot path on GB300 (one JSON line on stdout, rank 0).
+
+Workload ("ch4_radial_scan_590"): the CH4 system of the benchmark configurations -- C + 4 H,
+27 primitives, DM2 from a seeded closed-shell 1-RDM with 5 orbitals, all 142 884 quartets --
+evaluated as radial_plot with s = 0..10 bohr step 0.05 (201 shells) at nang = 590
+(62 390 grid points), thresh 1e-12, plus the same system's radial integral (nrad 50, nang 110)
+for the FP64-vs-mixed comparison. Inputs are synthetic (seeded); see
+inca_parallel_gb300/workloads.py.
+
+A step is one pass of the hot path with the quartet records and the grid resident in HBM:
+screening/set-up of every quartet (inca_prepare), the evaluation of all surviving quartets at
+every grid point (inca_eval, mixed FP32/FP64 form at tolerance 1e-8 relative per I(s)) and
+the I(s) reduction. value = (survivors x grid points) / step time. The records and grid fit
+in L2, so L2 is flushed (256 MiB write) before every timed step, outside the event bracket.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "quartet-point evals/s"
+THRESH = 1e-12
+SCAN = dict(start=[0.0], end=[10.0], step=[0.05], nang=[590])
+TOL_SCAN = 1e-8
+TOL_INTEGRAL = 1e-10
+FP32_LANES_PER_SM = 128
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload():
+    from inca_parallel_gb300 import workloads as W
+    b = W.ch4_basis()
+    D, S = W.closed_shell_density(b, 5, W.SEED0 + 0)
+    ijkl, v = W.folded_records(D)
+    return b, D, ijkl, v
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle port)
+def cpu_rate(b, ijkl, v, seconds):
+    """The oracle (C++ FP64 restatement of the reference loop, OpenMP on all host cores) on a
+    bounded sample of the scan grid; returns quartet-point evals/s and the sample used."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    sys_ = {"alpha": b["alpha"], "tmn": b["tmn"], "xyz": b["xyz"], "ijkl": ijkl, "v": v}
+    g = O.gridpoints2(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+    pts = g["r"]
+    n = 64
+    while True:
+        idx = np.linspace(0, len(pts) - 1, n).astype(int)
+        t0 = time.perf_counter()
+        _, cnt = O.intracule(sys_, THRESH, pts[idx])
+        dt = time.perf_counter() - t0
+        if dt > seconds / 4 or n >= len(pts):
+            break
+        n = min(len(pts), int(n * max(2.0, (seconds / 4) / max(dt, 1e-3))))
+    reps = max(1, int(seconds / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.intracule(sys_, THRESH, pts[idx])
+    dt = (time.perf_counter() - t0) / reps
+    qp = cnt[2] * len(idx)
+    return qp / dt, {"points": int(len(idx)), "of_points": int(len(pts)), "survivors": int(cnt[2]),
+                     "repeats": reps, "seconds_per_sample": dt}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    b, D, ijkl, v = workload()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    per_step = max(2.0, min(args.cpu_seconds, 60.0) / max(1, args.steps))
+    rates = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        r, sample = cpu_rate(b, ijkl, v, per_step)
+        if i >= args.warmup:
+            rates.append(r)
+    val = statistics.median(rates)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "quartet-points/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CH4 closed-shell DM2)",
+            "config": {"workload": "ch4_radial_scan_590", "points": 62390, "quartets": int(len(v)),
+                       "cpu_sample": sample},
+            "cpu_baseline": {"value": val, "unit": "quartet-points/s", "cores": cores, "kind": "port",
+                             "sample": f"oracle (C++ FP64 restatement of the reference OpenMP loop) on "
+                                       f"{sample['points']} of {sample['of_points']} scan points, all quartets"},
+            "e2e": {"value": val, "unit": "quartet-points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from inca_parallel_gb300 import INCA_FP64, INCA_MIXED, Context
+    b, D, ijkl, v = workload()
+    ctx = Context(local)
+    ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+    ctx.set_quartets(ijkl, v)
+    counts = ctx.prepare(THRESH)
+    nradi, ngrid = ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+    rec = ctx.records()
+    Lbar = float(rec["L"].sum(axis=1).mean())
+    qp = counts[2] * ngrid
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def step(mode, tol):
+        ctx.prepare(THRESH)
+        ctx.eval(mode=mode, tol=tol, copy=False)
+        return ctx.radial_plot()[1]
+
+    def timed(mode, tol, k, w):
+        for _ in range(w):
+            step(mode, tol)
+        times, kern = [], []
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t_wall = time.perf_counter()
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = step(mode, tol)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            kern.append(ctx.timing())
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return times, kern, time.perf_counter() - t_wall, out
+
+    # FP64 reference form (plain GPU form), fewer steps (it is ~2 orders slower)
+    t64, k64, _, I64 = timed(INCA_FP64, 0.0, max(2, args.steps // 3), 1)
+    # mixed form: the headline
+    launches0 = ctx.kernel_launches()
+    with ClockSampler(local) as clk:
+        tm, km, wall, Imix = timed(INCA_MIXED, TOL_SCAN, args.steps, args.warmup)
+    launches = (ctx.kernel_launches() - launches0) // (args.steps + args.warmup)
+    stats = ctx.stats()
+    ms = statistics.mean(tm)
+    ms64 = statistics.mean(t64)
+    rel_scan = float(np.max(np.abs(Imix - I64) / np.abs(I64)))
+    # radial integral (nrad 50, nang 110, multicentre centres of CH4): time and error, both forms
+    from inca_parallel_gb300 import centercalc
+    cent, Ps, alf = centercalc(b["an"], b["cartes"])
+    ctx.grid_radial([50] * len(Ps), [110] * len(Ps), alf, cent, Ps)
+    ri = {}
+    for name, mode in (("fp64", INCA_FP64), ("mixed", INCA_MIXED)):
+        ts = []
+        for i in range(4):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.prepare(THRESH)
+            ctx.eval(mode=mode, tol=TOL_INTEGRAL, copy=False)
+            val = ctx.radial_integral()[0]
+            e1.record(stream)
+            e1.synchronize()
+            if i:
+                ts.append(e0.elapsed_time(e1))
+        ri[name] = {"ms": statistics.mean(ts), "value": val}
+    ri_rel = abs(ri["mixed"]["value"] - ri["fp64"]["value"]) / abs(ri["fp64"]["value"])
+
+    # end to end through the C ABI with host buffers (the driver's call sequence)
+    ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+    h2d = int(ijkl.nbytes + v.nbytes + b["alpha"].nbytes * 4 + b["tmn"].nbytes)
+    d2h = int(8 * ngrid + 8 * nradi)
+    e2e_t = []
+    for i in range(2 + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+        ctx.set_quartets(ijkl, v)
+        ctx.prepare(THRESH)
+        ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+        ctx.eval(mode=INCA_MIXED, tol=TOL_SCAN, copy=True)
+        ctx.radial_plot()
+        torch.cuda.synchronize()
+        if i >= 2:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+
+    # roofline of the dominant kernel (k_mixed): algorithmic FP32 flops per launch / launch time
+    kms = statistics.mean(k["kernel_ms"] for k in km) / 2.0  # two launches (estimate + tiered)
+    flops_per_qp = 17.0 + 2.0 * Lbar
+    achieved = qp * flops_per_qp / (kms * 1e-3) / 1e12
+    csum = clk.summary()
+    sm_mhz = csum["sm_mhz"] or 2070.0
+    peak = 152 * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    cpu_val, cpu_sample, cores = None, None, os.cpu_count() or 1
+    if rank == 0 and world == 1:
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        cpu_val, cpu_sample = cpu_rate(b, ijkl, v, args.cpu_seconds)
+
+    # whole-job aggregate: max time over ranks (each rank evaluates its own copy: weak scaling)
+    t_step = ms
+    if world > 1:
+        tt = torch.tensor([t_step], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = world * qp / (t_step * 1e-3)
+    if rank == 0:
+        prof = os.path.join(ROOT, "profiles", "k_mixed_ch4_radial_scan_590.md")
+        traffic = None
+        if os.path.exists(prof):
+            for ln in open(prof):
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    traffic = float(ln.split(":")[1])
+        line = {
+            "metric": METRIC, "value": value, "unit": "quartet-points/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-evaluate/f64-accumulate (FP64 precise tier)",
+            "data": "synthetic (seeded CH4 closed-shell DM2, 5 orbitals)",
+            "config": {"workload": "ch4_radial_scan_590", "system": "CH4 27 primitives", "quartets": int(counts[0]),
+                       "survivors": int(counts[2]), "grid_points": int(ngrid), "shells": int(nradi), "nang": 590,
+                       "thresh": THRESH, "tolerance_I_s": TOL_SCAN, "l2": "flushed before each step (256 MiB write)",
+                       "mean_L": Lbar,
+                       "fp64_form": {"ms_per_step": ms64, "value": qp / (ms64 * 1e-3)},
+                       "speedup_vs_fp64_form": ms64 / ms, "max_rel_err_I_s_vs_fp64": rel_scan,
+                       "tiers": stats,
+                       "radial_integral_nrad50_nang110": {"fp64_ms": ri["fp64"]["ms"], "mixed_ms": ri["mixed"]["ms"],
+                                                          "rel_err": ri_rel, "value": ri["fp64"]["value"],
+                                                          "tolerance": TOL_INTEGRAL}},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_mixed", "kernel_ms_per_launch": kms,
+                         "flops_per_quartet_point": flops_per_qp,
+                         "peak_source": "152 SMs x 128 FP32 lanes x 2 (FMA) x median sampled SM clock"},
+            "clocks": csum,
+            "e2e": {"value": qp / e2e_s, "unit": "quartet-points/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": int(launches),
+        }
+        if cpu_val is not None:
+            line["cpu_baseline"] = {"value": cpu_val, "unit": "quartet-points/s", "cores": cores, "kind": "port",
+                                    "sample": f"oracle (C++ FP64, OpenMP) on {cpu_sample['points']} of "
+                                              f"{cpu_sample['of_points']} scan points, all {cpu_sample['survivors']} "
+                                              f"surviving quartets"}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+// Internal declarations of libinca_gpu.so (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/inca_gpu.h"
+
+namespace inca {
+
+constexpr int kMaxDeg = INCA_MAX_DEGREE;  // per-dimension polynomial degree
+constexpr int kMaxCoef = kMaxDeg + 1;
+constexpr int kRecHeader = 6;             // A, sqe, d0, d1, d2, B (term bound factor)
+constexpr int kMaxGH = 11;                // Gauss-Hermite nodes for L <= 21
+
+// ---------------------------------------------------------------- status helpers
+struct Error {
+  int code;
+  std::string msg;
+};
+
+// Device buffer owned by the context; grows, never shrinks until the context dies.
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;  // capacity in elements
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (want == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), want * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// One primitive as the device kernels read it.
+struct PrimD {
+  double alpha, x, y, z, norm;
+  int t[3];
+  int pad;
+};
+
+// Angular class of survivors: all records of a class share (Lx, Ly, Lz) and a stride.
+struct ClassSeg {
+  int L[3];
+  int stride;       // doubles per FP64 record (even)
+  int64_t first;    // first survivor (class-sorted index)
+  int64_t count;
+  int64_t off64;    // offset of the segment in the FP64 record array (doubles)
+  int64_t off32;    // offset of the segment in the FP32 record array (floats)
+  int stride32;     // floats per FP32 record (multiple of 4)
+  int pad;
+};
+
+// A chunk of <= kChunk records of one class: the unit of work of the evaluation kernels.
+struct WorkChunk {
+  int cls;
+  int count;
+  int64_t rec;  // first class-sorted survivor index
+};
+
+enum GridKind { GRID_NONE = 0, GRID_RADIAL = 1, GRID_SCAN = 2, GRID_CUBE = 3, GRID_POINTS = 4 };
+
+}  // namespace inca
+
+struct inca_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // primitives
+  int nprim = 0;
+  std::vector<double> h_alpha, h_x, h_y, h_z;
+  std::vector<int> h_tmn;  // row-major nprim x 3
+  inca::DevBuf<inca::PrimD> d_prims;
+
+  // quartet input (device, 1-based indices)
+  int64_t nq = 0;
+  inca::DevBuf<int4> d_ijkl;
+  inca::DevBuf<double> d_v;
+
+  // screening results in input order
+  bool prepared = false;
+  inca_counts counts{0, 0, 0};
+  double lim = 0.0;
+  inca::DevBuf<uint8_t> d_flags;
+  inca::DevBuf<double> d_s1, d_s2;
+  bool have_screen_values = false;
+
+  // survivors, grouped by class
+  int64_t nsurv = 0;
+  std::vector<inca::ClassSeg> classes;
+  std::vector<inca::WorkChunk> chunks;
+  inca::DevBuf<inca::ClassSeg> d_classes;
+  inca::DevBuf<inca::WorkChunk> d_chunks;
+  inca::DevBuf<double> d_rec64;     // FP64 records, class segments
+  inca::DevBuf<float> d_rec32;      // FP32 records (mixed form), class segments
+  inca::DevBuf<int64_t> d_surv_src; // input index of each class-sorted survivor
+  int max_L = 0;
+
+  // grid
+  int grid_kind = inca::GRID_NONE;
+  int64_t ngrid = 0, maxgrid = 0, rgrid = 0;
+  int nquad = 0;
+  int nradi = 0;
+  std::vector<int> h_smn;        // points per shell (scan grids)
+  std::vector<double> h_radi;    // shell radii (scan grids)
+  std::vector<double> h_cent;    // centres (radial grids)
+  inca::DevBuf<double> d_px, d_py, d_pz, d_w, d_wvee;
+  inca::DevBuf<int> d_cmap;
+  inca::DevBuf<double> d_ivec;
+  bool evaluated = false;
+
+  // scratch
+  inca::DevBuf<double> d_partial;
+  inca::DevBuf<unsigned char> d_scratch;
+
+  // timing and tier statistics of the last evaluation
+  double t_total_ms = 0, t_kernel_ms = 0;
+  int t_kernel_launches = 0, t_launches = 0;
+  int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0;
+  int64_t launches = 0;  // own kernel launches since creation
+};
+
+// ---- internal entry points between translation units
+namespace inca {
+
+int set_error(inca_ctx* c, int code, const std::string& msg);
+int cuda_error(inca_ctx* c, cudaError_t e, const char* what);
+
+// quartet_prep.cu
+int prepare_device(inca_ctx* c, double thresh, int normalize);
+int gen_closed_shell_device(inca_ctx* c, const double* D, int unique, int64_t* nrec);
+
+// intracule_eval.cu
+int eval_device(inca_ctx* c, int mode, double tol);
+
+// grid_build.cu
+int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,
+                       const double* sfalpha, const double* cent, const double* Ps, int nosym);
+int grid_scan_device(inca_ctx* c, int nblock, const double* start, const double* end,
+                     const double* step, const int* nang, int nosym);
+int grid_cube_device(inca_ctx* c, const double* center, const double* step, const int* np);
+int radial_integral_device(inca_ctx* c, double* total, double* vee, double* per_c, double* vee_c);
+int radial_plot_device(inca_ctx* c, double* rintra);
+int smearing_device(inca_ctx* c, double u_max, int n_bins, double sigma, double* u, double* P,
+                    double* I);
+
+// host_tables.cpp
+int lebedev_rule(int nang, std::vector<double>& x, std::vector<double>& y,
+                 std::vector<double>& z, std::vector<double>& w);
+void gauss_legendre(int n, double* t, double* w);
+int read_dm2p(const char* path, int nprim, std::vector<int4>& ijkl, std::vector<double>& v,
+              std::string& err);
+
+}  // namespace inca
+
+// Launch one of this library's kernels on the context stream and count it.
+#define INCA_LAUNCH(c, kernel, grid, block, smem, ...)                          \
+  do {                                                                         \
+    kernel<<<(grid), (block), (smem), (c)->stream>>>(__VA_ARGS__);             \
+    ++(c)->launches;                                                           \
+  } while (0)
+
+#define INCA_CUDA(c, call)                                        \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return inca::cuda_error((c), e_, #call); \
+  } while (0)

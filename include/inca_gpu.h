@@ -1,0 +1,177 @@
+/*
+ * inca_gpu.h -- C ABI of the GB300 intracule engine (libinca_gpu.so).
+ *
+ * Drop-in boundary for the intracule hot path of INCA (markelgtx/INCA_parallel). In the
+ * reference that path is one Fortran subroutine, calculate_intracule(normalize_dm2p)
+ * (src/mod_intracule.f90:18-572), fed through module globals and called once from the
+ * main program (src/inca_main.f90:76). This header replaces it with plain C entry points
+ * that a Fortran bind(C) interface, the C++ driver or ctypes can call. Conventions:
+ *
+ *  - The caller owns every host array; outputs go into caller-provided buffers.
+ *  - Every call returns an int status (INCA_OK == 0). On failure inca_last_error(ctx)
+ *    returns a message; the Fortran side prints it and stops, as the reference does.
+ *  - Primitive and quartet indices are 1-based at the boundary, as in the .dm2p file.
+ *  - Arrays shaped like Fortran arrays are column-major: TMN(nprim,3), r(3,ngrid),
+ *    cartes(natoms,3).
+ *  - One context per host thread; calls are synchronous (results are on the host when a
+ *    call returns). A context owns one CUDA stream on one device.
+ *  - No CPU fallback: a context cannot be created without a usable sm_103 device.
+ */
+#ifndef INCA_GPU_H
+#define INCA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define INCA_ABI_VERSION 1
+
+/* status codes */
+#define INCA_OK 0
+#define INCA_E_ARG 1     /* invalid argument: null pointer, bad size, unsupported rule   */
+#define INCA_E_CUDA 2    /* CUDA runtime error (the message carries the CUDA string)      */
+#define INCA_E_IO 3      /* file could not be opened or read                              */
+#define INCA_E_FORMAT 4  /* unsupported or corrupt .dm2p content                          */
+#define INCA_E_STATE 5   /* call order violated (e.g. evaluation before inca_prepare)     */
+#define INCA_E_NOMEM 6   /* device memory exhausted                                       */
+#define INCA_E_LIMIT 7   /* size beyond a documented maximum (e.g. per-dimension degree)  */
+#define INCA_E_TIMEOUT 8 /* a bounded device wait gave up; the context stays usable       */
+
+/* evaluation precision */
+#define INCA_FP64 0  /* every quartet-point term in FP64 (the plain GPU form)              */
+#define INCA_MIXED 1 /* FP32 terms with FP64 accumulation; terms whose FP32 error could
+                        exceed the requested tolerance are evaluated in FP64             */
+
+/* maximum per-dimension polynomial degree t_i+t_j+t_k+t_l (g shells: 16) */
+#define INCA_MAX_DEGREE 16
+
+typedef struct inca_ctx inca_ctx;
+
+/* Quartet counts as reported in the .out file (src/mod_intracule.f90:419-421). */
+typedef struct inca_counts {
+  int64_t read;          /* "Quartets in the dm2p file"   */
+  int64_t after_screen1; /* "Quartets after 1st screening" */
+  int64_t after_screen2; /* "Quartets actually computed"   */
+} inca_counts;
+
+int inca_abi_version(void);
+
+/* Context on a CUDA device (the OpenMP team of mod_intracule.f90:203-388 becomes one GPU). */
+int inca_ctx_create(inca_ctx** ctx, int device);
+int inca_ctx_destroy(inca_ctx* ctx);
+const char* inca_last_error(const inca_ctx* ctx);
+
+/* Primitive basis in .dm2p order: Alpha, TMN, Xn/Yn/Zn of mod_geninfo
+ * (src/mod_geninfo.f90:9-19, filled by filebas, src/mod_read_files.f90:695-726). */
+int inca_set_primitives(inca_ctx* ctx, int32_t nprim, const double* alpha, const int32_t* tmn,
+                        const double* xn, const double* yn, const double* zn);
+
+/* DM2 quartets. Replaces the batched .dm2p read (src/mod_intracule.f90:164-262): the same
+ * format sniffing (flat stream, or sequential records with 4-byte markers); reading stops
+ * at end of file or at the first record whose index is out of range, as in the reference.
+ * Formats with 8-byte or zero markers fail with INCA_E_FORMAT. nread may be NULL. */
+int inca_load_dm2p(inca_ctx* ctx, const char* path, int64_t* nread);
+
+/* Quartets from memory: ijkl[4*q+0..3] = i,j,k,l (1-based), v[q] = DM2 value. */
+int inca_set_quartets(inca_ctx* ctx, int64_t n, const int32_t* ijkl, const double* v);
+
+/* Closed-shell DM2 from a 1-RDM D(nprim,nprim) (column-major, primitive basis):
+ * Gamma_{ik,jl} = D_ik D_jl - 1/2 D_il D_jk, folded into records with i<=k and j<=l.
+ * unique != 0 additionally folds (ik)<->(jl), keeping pair(ik) <= pair(jl)
+ * (a symmetry-unique list: evaluate it with nosym). The records are generated on the device. */
+int inca_gen_closed_shell_dm2(inca_ctx* ctx, const double* D, int unique, int64_t* nrecords);
+
+/* Screening and per-quartet set-up on the device (src/mod_intracule.f90:282-343 with
+ * JA8/polycoef of src/mod_intrastuff.f90:32-194): normalisation (normalize != 0, as
+ * calculate_intracule(.true.)), screen 1, Gaussian products, the three polynomial
+ * coefficient vectors (LU with partial pivoting), screen 2. lim = thresh/(nprim(nprim+1)/2).
+ * The survivors stay resident on the device, grouped by angular class. counts may be NULL. */
+int inca_prepare(inca_ctx* ctx, double thresh, int normalize, inca_counts* counts);
+
+/* Per-quartet screening results of the last inca_prepare, in input order (for checks):
+ * flags[q] = 0 (fails screen 1), 1 (passes 1, fails 2), 3 (passes both); s1/s2 values.
+ * Any pointer may be NULL. */
+int inca_get_screening(inca_ctx* ctx, uint8_t* flags, double* s1, double* s2);
+
+/* Survivor records of the last inca_prepare in input order: A, sqe, d = P_ik - P_jl (3),
+ * L (3) and coefficients C (3 x 17, highest degree first). Any pointer may be NULL. */
+int inca_get_records(inca_ctx* ctx, double* A, double* sqe, double* d, int32_t* L, double* C);
+
+/* ---- grids, built and kept on the device (src/mod_build_grid.f90) ---- */
+
+/* Multicentre radial x Lebedev grid with TFVC weights (gridpoints + becke, lines 13-277 and
+ * 474-575). cent is cent(3,nquad). Outputs: maxgrid (before halving), rgrid (after
+ * symmetry halving), ngrid (after dropping weights <= 1e-106). */
+int inca_grid_radial(inca_ctx* ctx, int32_t nquad, const int32_t* nradc, const int32_t* nangc,
+                     const double* sfalpha, const double* cent, const double* Ps, int nosym,
+                     int64_t* maxgrid, int64_t* rgrid, int64_t* ngrid);
+
+/* Radial-scan shells for I(s) (gridpoints2, lines 281-408). */
+int inca_grid_scan(inca_ctx* ctx, int32_t nblock, const double* start, const double* end,
+                   const double* step, const int32_t* nang, int nosym, int32_t* nradi,
+                   int64_t* ngrid);
+
+/* Uniform lattice for the vector cube, x outer / z inner (gridpoints3, lines 412-440). */
+int inca_grid_cube(inca_ctx* ctx, const double* center, const double* step, const int32_t* np,
+                   int64_t* ngrid);
+
+/* Explicit points r(3,n) (intracule_at_zero, intracule_two_points, mod_intracule.f90:114-129). */
+int inca_grid_points(inca_ctx* ctx, int64_t n, const double* r);
+
+/* Copy the resident grid to the host: r(3,ngrid), weights, Vee weights, centre index
+ * (1-based) for radial grids; angular weights in w for scan grids. Pointers may be NULL. */
+int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* cmap);
+
+/* ---- evaluation and reductions ---- */
+
+/* Evaluate I at every point of the resident grid (mod_intracule.f90:345-358, all quartets).
+ * mode: INCA_FP64 or INCA_MIXED; tol: relative tolerance of the mixed form on the grid's
+ * outputs (ignored for INCA_FP64; <= 0 selects 1e-10). ivec (ngrid) may be NULL (result
+ * stays on the device for the reductions). */
+int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
+
+/* Radial integral, Vee and the per-centre TFVC decomposition (mod_intracule.f90:441-455)
+ * of the last evaluation on a radial grid. per_centre/vee_per_centre (nquad) may be NULL. */
+int inca_radial_integral(inca_ctx* ctx, double* total, double* vee, double* per_centre,
+                         double* vee_per_centre);
+
+/* I(s) per shell of the last evaluation on a scan grid (mod_intracule.f90:522-530). */
+int inca_radial_plot(inca_ctx* ctx, double* radi, double* rintra);
+
+/* Gaussian-smeared P(u) and I_avg(u) of the last radial-grid evaluation
+ * (radial_smearing, mod_intracule.f90:576-649): n_bins values each. */
+int inca_radial_smearing(inca_ctx* ctx, double u_max, int32_t n_bins, double sigma,
+                         double* u_axis, double* P_u, double* I_avg);
+
+/* Automatic integration centres (centercalc + get_bs_radius, src/mod_autogrid.f90:12-185).
+ * an(natoms), cartes(natoms,3) in bohr. Output capacity: natoms*(natoms-1)+1 centres;
+ * cent(3,nquad). Host-side (tiny). */
+int inca_centercalc(int32_t natoms, const int32_t* an, const double* cartes, int nohydro,
+                    int betaone, int32_t* nquad, double* cent, double* Ps, double* sfalpha);
+
+/* Timing of the last inca_eval on the device (CUDA events): total milliseconds, the
+ * milliseconds of its dominant kernel, the number of that kernel's launches and the
+ * number of kernel launches of the call. Pointers may be NULL. */
+int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
+                          int32_t* kernel_launches, int32_t* launches);
+
+/* Work split of the last INCA_MIXED evaluation, in (quartet, point tile) pairs: evaluated in
+ * FP32, evaluated in FP64 (precise tier), skipped (bounded below the tolerance). The FP64
+ * form reports zeros. Pointers may be NULL. */
+int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* fp64_pairs,
+                         int64_t* skipped_pairs);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work or
+ * record CUDA events around the library's calls. */
+int inca_get_stream(inca_ctx* ctx, void** stream);
+
+/* Number of this library's own kernels launched by the context since it was created
+ * (library kernels such as CUB sorts are not counted). */
+int inca_kernel_launches(inca_ctx* ctx, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* INCA_GPU_H */

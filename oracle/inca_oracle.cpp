@@ -27,6 +27,7 @@
 namespace {
 
 const double kPi = 4.0 * std::atan(1.0);  // mod_numbers.f90:6
+const double kPi15 = kPi * std::sqrt(kPi); // pi**1.5 (mod_intrastuff.f90:115)
 const int kMaxDeg = 16;                    // per-dimension polynomial degree (g shells)
 const int kMaxCoef = kMaxDeg + 1;
 
@@ -137,6 +138,39 @@ int lebedev(int nang, std::vector<double>& x, std::vector<double>& y, std::vecto
   return (int)x.size() == nang ? 0 : -1;
 }
 
+// ---- Deterministic FP64 arithmetic for the screening quantities.
+// The reference evaluates its bounds with Fortran ** and dexp (libm). The oracle fixes the
+// operation sequence instead, so the GPU's screening can be checked bit for bit:
+//  * x**n for integer n >= 0: left-to-right repeated multiplication (x**0 = 1);
+//  * exp: Cody-Waite reduction x = k ln2 + r (ln2 split in a 32-bit head and a tail),
+//    Taylor polynomial of degree 13 for e^r by Horner, scaled by 2^k.
+// Compiled without FMA contraction; the results differ from libm by at most a few ulp.
+double ipow(double x, int n) {
+  if (n <= 0) return 1.0;
+  double r = x;
+  for (int i = 1; i < n; ++i) r = r * x;
+  return r;
+}
+
+double pexp(double x) {
+  if (x != x) return x;
+  if (x > 709.0) return HUGE_VAL;
+  if (x < -708.0) return 0.0;  // no subnormal results
+  const double kInvLn2 = 1.4426950408889634;
+  const double kLn2Hi = 0.6931471803691238;      // 0x1.62e42feep-1: 32 significant bits
+  const double kLn2Lo = 1.9082149292705877e-10;  // ln 2 - kLn2Hi
+  double k = std::nearbyint(x * kInvLn2);
+  double r = (x - k * kLn2Hi) - k * kLn2Lo;
+  // 1/i! for i = 13..0, correctly rounded
+  static const double c[14] = {1.6059043836821613e-10, 2.08767569878681e-09, 2.505210838544172e-08,
+                               2.755731922398589e-07, 2.7557319223985893e-06, 2.48015873015873e-05,
+                               0.0001984126984126984, 0.001388888888888889, 0.008333333333333333,
+                               0.041666666666666664, 0.16666666666666666, 0.5, 1.0, 1.0};
+  double p = c[0];
+  for (int i = 1; i < 14; ++i) p = p * r + c[i];
+  return std::ldexp(p, (int)k);
+}
+
 // Number of Gauss-Hermite nodes for total power L (mod_intrastuff.f90:210-220).
 inline int gh_nodes(int L) { return L / 2 + 1; }
 
@@ -153,13 +187,15 @@ struct Prim {
 double ja8(const Prim& pi_, const Prim& pk, double Rik2, double aik, double eik) {
   int sumt = pi_.t[0] + pk.t[0] + pi_.t[1] + pk.t[1] + pi_.t[2] + pk.t[2];
   double s2a = std::sqrt(2.0 / aik);
-  double v = std::pow(kPi, 1.5) * std::pow(2.0 * aik, -(double(sumt) + 1.5)) *
-             std::exp(-2.0 * eik * Rik2);
+  // pi^1.5 (2 aik)^-(sumt+1.5) e^(-2 eik Rik2) with (2a)^-(s+1.5) = 1/((2a)^(s+1) sqrt(2a))
+  double two_a = 2.0 * aik;
+  double v = kPi15 / (ipow(two_a, sumt + 1) * std::sqrt(two_a));
+  v = v * pexp((-2.0 * eik) * Rik2);
   for (int d = 0; d < 3; ++d) {
     double xm = hermite_xmax(pi_.t[d] + pk.t[d] + 1);
     double dx = std::fabs(pk.x[d] - pi_.x[d]);
-    v *= std::pow(xm + pk.alpha * s2a * dx, 2.0 * double(pi_.t[d]));
-    v *= std::pow(xm + pi_.alpha * s2a * dx, 2.0 * double(pk.t[d]));
+    v = v * ipow(xm + (pk.alpha * s2a) * dx, 2 * pi_.t[d]);
+    v = v * ipow(xm + (pi_.alpha * s2a) * dx, 2 * pk.t[d]);
   }
   return v;
 }
@@ -219,17 +255,16 @@ int polycoef(const double R[4], double Pik, double Pjl, double Pijkl, const int 
   double M[kMaxCoef * kMaxCoef];
   for (int i = 0; i < np; ++i) {
     double xx = -0.5 + double(i + 1);
-    double base = sqe * (xx + Pik - Pjl);
-    for (int j = 0; j < np; ++j) M[i * np + j] = std::pow(base, double(L - j));
+    double base = sqe * ((xx + Pik) - Pjl);
+    for (int j = 0; j < np; ++j) M[i * np + j] = ipow(base, L - j);
     double rhs = 0.0;
     double am = (alf - 0.5) * xx, ap = (alf + 0.5) * xx;
     for (int h = 0; h < nn; ++h) {
       double zr = invz * rh[h];
-      double W = std::pow(zr + am + (Pijkl - R[0]), double(t[0])) *
-                 std::pow(zr + ap + (Pijkl - R[1]), double(t[1])) *
-                 std::pow(zr + am + (Pijkl - R[2]), double(t[2])) *
-                 std::pow(zr + ap + (Pijkl - R[3]), double(t[3]));
-      rhs += wh[h] * W;
+      double W = ipow((zr + am) + (Pijkl - R[0]), t[0]) * ipow((zr + ap) + (Pijkl - R[1]), t[1]);
+      W = W * ipow((zr + am) + (Pijkl - R[2]), t[2]);
+      W = W * ipow((zr + ap) + (Pijkl - R[3]), t[3]);
+      rhs = rhs + wh[h] * W;
     }
     C[i] = rhs;
   }
@@ -309,8 +344,9 @@ int prepare_one(const Setup& S, int i, int j, int k, int l, double v, Quartet* q
   }
   for (int d = 0; d < 3; ++d) Pijkl[d] = (aik * Pik[d] + ajl * Pjl[d]) * (1.0 / zeta);
   double invz = 1.0 / std::sqrt(zeta);
-  double alf = 0.5 * (aik - ajl) * (1.0 / zeta);
-  double A = DMval * std::pow(zeta, -1.5) * std::exp(-eik * Rik2 - ejl * Rjl2);
+  double alf = (0.5 * (aik - ajl)) * (1.0 / zeta);
+  double A = DMval * (1.0 / (zeta * std::sqrt(zeta)));
+  A = A * pexp((-eik) * Rik2 - ejl * Rjl2);
   Quartet Q;
   double U[3];
   for (int d = 0; d < 3; ++d) {
@@ -319,9 +355,9 @@ int prepare_one(const Setup& S, int i, int j, int k, int l, double v, Quartet* q
     Q.L[d] = t[0] + t[1] + t[2] + t[3];
     polycoef(R, Pik[d], Pjl[d], Pijkl[d], t, sqe, invz, alf, Q.C[d]);
     U[d] = 0.0;
-    for (int m = 0; m <= Q.L[d]; ++m) U[d] += Q.C[d][m] * S.wm[m];
+    for (int m = 0; m <= Q.L[d]; ++m) U[d] = U[d] + Q.C[d][m] * S.wm[m];
   }
-  double screen2 = std::fabs(A * U[0] * U[1] * U[2]);
+  double screen2 = std::fabs(((A * U[0]) * U[1]) * U[2]);
   if (s2out) *s2out = screen2;
   if (!(screen2 >= S.lim)) return 1;
   Q.A = A;
