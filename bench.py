@@ -211,7 +211,7 @@ def gpu_arm(args):
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            kern.append(ctx.timing())
+            kern.append(ctx.phases())
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -270,8 +270,10 @@ def gpu_arm(args):
             e2e_t.append(time.perf_counter() - t0)
     e2e_s = statistics.mean(e2e_t)
 
-    # roofline of the dominant kernel (k_mixed): algorithmic FP32 flops per launch / launch time
-    kms = statistics.mean(k["kernel_ms"] for k in km) / 2.0  # two launches (estimate + tiered)
+    # roofline of the dominant kernel (k_pass1: every term in FP32): algorithmic FP32 flops of
+    # one launch (all quartet-points, 17 + 2 L flops each) / its CUDA-event duration
+    kms = statistics.mean(k["pass1_ms"] for k in km)
+    pass2_ms = statistics.mean(k["pass2_ms"] for k in km)
     flops_per_qp = 17.0 + 2.0 * Lbar
     achieved = qp * flops_per_qp / (kms * 1e-3) / 1e12
     csum = clk.summary()
@@ -290,7 +292,7 @@ def gpu_arm(args):
         t_step = float(tt.item())
     value = world * qp / (t_step * 1e-3)
     if rank == 0:
-        prof = os.path.join(ROOT, "profiles", "k_mixed_ch4_radial_scan_590.md")
+        prof = os.path.join(ROOT, "profiles", "k_pass1_ch4_radial_scan_590.md")
         traffic = None
         if os.path.exists(prof):
             for ln in open(prof):
@@ -299,7 +301,7 @@ def gpu_arm(args):
         line = {
             "metric": METRIC, "value": value, "unit": "quartet-points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32-evaluate/f64-accumulate (FP64 precise tier)",
+            "vs_baseline": None, "dtype": "f32 (double-float correction tier, f64 accumulation)",
             "data": "synthetic (seeded CH4 closed-shell DM2, 5 orbitals)",
             "config": {"workload": "ch4_radial_scan_590", "system": "CH4 27 primitives", "quartets": int(counts[0]),
                        "survivors": int(counts[2]), "grid_points": int(ngrid), "shells": int(nradi), "nang": 590,
@@ -313,7 +315,7 @@ def gpu_arm(args):
                                                           "tolerance": TOL_INTEGRAL}},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_mixed", "kernel_ms_per_launch": kms,
+                         "kernel": "k_pass1", "kernel_ms_per_launch": kms, "pass2_ms": pass2_ms,
                          "flops_per_quartet_point": flops_per_qp,
                          "peak_source": "152 SMs x 128 FP32 lanes x 2 (FMA) x median sampled SM clock"},
             "clocks": csum,

@@ -55,6 +55,7 @@ SIGNATURES = {
     "inca_last_eval_timing": (ctypes.c_int, [VP, DP, DP, IP, IP]),
     "inca_last_eval_stats": (ctypes.c_int, [VP, I64P, I64P, I64P]),
     "inca_get_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
+    "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
 }
 
@@ -271,7 +272,12 @@ class Context:
     def stats(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         self._check(self.lib.inca_last_eval_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"fp32_pairs": a.value, "fp64_pairs": b.value, "skipped_pairs": c.value}
+        return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value}
+
+    def phases(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.inca_last_eval_phases(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return {"pass1_ms": a.value, "pass2_ms": b.value}
 
 
 def centercalc(an, cartes, nohydro=True, betaone=False):

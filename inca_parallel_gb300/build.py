@@ -27,7 +27,7 @@ UNITS = {
     "quartet_prep.cu": ["-fmad=false"],
     "intracule_eval.cu": [],
     "mixed_eval.cu": [],
-    "grid_build.cu": [],
+    "grid_build.cu": ["-fmad=false"],
     "host_tables.cpp": [],
 }
 DRIVER_SRC = os.path.join(CSRC, "driver", "inca_main.cpp")

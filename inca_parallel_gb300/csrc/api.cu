@@ -84,6 +84,10 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_ivec.release();
   c->d_partial.release();
   c->d_scratch.release();
+  c->d_phi.release();
+  c->d_plo.release();
+  c->d_perm.release();
+  c->d_wtbox.release();
   cudaStreamDestroy(c->stream);
   delete c;
   return INCA_OK;
@@ -285,6 +289,7 @@ int inca_grid_points(inca_ctx* c, int64_t n, const double* r) {
   c->grid_kind = GRID_POINTS;
   c->ngrid = c->rgrid = c->maxgrid = n;
   c->evaluated = false;
+  ++c->grid_version;
   return INCA_OK;
 }
 
@@ -363,6 +368,13 @@ int inca_last_eval_stats(inca_ctx* c, int64_t* fp32_pairs, int64_t* fp64_pairs, 
   if (fp32_pairs) *fp32_pairs = c->pairs_fp32;
   if (fp64_pairs) *fp64_pairs = c->pairs_fp64;
   if (skipped_pairs) *skipped_pairs = c->pairs_skip;
+  return INCA_OK;
+}
+
+int inca_last_eval_phases(inca_ctx* c, double* pass1_ms, double* pass2_ms) {
+  if (!c) return INCA_E_ARG;
+  if (pass1_ms) *pass1_ms = c->t_kernel_ms;
+  if (pass2_ms) *pass2_ms = c->t_pass2_ms;
   return INCA_OK;
 }
 

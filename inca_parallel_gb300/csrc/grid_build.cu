@@ -1,6 +1,10 @@
 // K3: grids on the device (src/mod_build_grid.f90) and K4: the post-reductions of
 // calculate_intracule (src/mod_intracule.f90:441-455, 522-530, 576-649). FP64 throughout.
 //
+// This translation unit is compiled with -fmad=false: grid points and weights are then the
+// same bits as the CPU oracle's (an FMA-contracted x0 + s*i differs in the last place, which
+// can move a point across the 1e-106 weight cut or a z >= -tol test).
+//
 // Grids are stored as FP64 structure-of-arrays (x, y, z, weight, Vee weight, centre) in the
 // reference's point order: centre-major, then radial node, then Lebedev point; shells in
 // order for the radial scan; x outer / z inner for the cube. Reductions are deterministic
@@ -82,7 +86,7 @@ __global__ void k_tfvc(int64_t n, const double* __restrict__ px, const double* _
       const double term = chi[i * nquad + j] * (1.0 - mu);
       double v = (1.0 + mu - term) / (1.0 + mu + term);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) v = 1.5 * v - 0.5 * (v * v * v);
+      for (int k = 0; k < 4; ++k) v = 1.5 * v - 0.5 * ((v * v) * v);
       P *= 0.5 * (1.0 - v);
     }
     ptot += P;
@@ -379,6 +383,7 @@ int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nang
   c->nquad = nquad;
   c->h_cent.assign(cent, cent + 3 * nquad);
   c->evaluated = false;
+  ++c->grid_version;
   return INCA_OK;
 }
 
@@ -458,6 +463,7 @@ int grid_scan_device(inca_ctx* c, int nblock, const double* start, const double*
   c->rgrid = n;
   c->maxgrid = ncand;
   c->evaluated = false;
+  ++c->grid_version;
   return INCA_OK;
 }
 
@@ -482,6 +488,7 @@ int grid_cube_device(inca_ctx* c, const double* center, const double* step, cons
   c->rgrid = n;
   c->maxgrid = n;
   c->evaluated = false;
+  ++c->grid_version;
   return INCA_OK;
 }
 

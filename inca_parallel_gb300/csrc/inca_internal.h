@@ -121,13 +121,20 @@ struct inca_ctx {
   inca::DevBuf<int> d_cmap;
   inca::DevBuf<double> d_ivec;
   bool evaluated = false;
+  int64_t grid_version = 0;  // bumped by every grid builder
+
+  // mixed evaluation: Morton-sorted copy of the grid (rebuilt when the grid changes)
+  int64_t mix_version = -1;
+  inca::DevBuf<float4> d_phi, d_plo;  // FP32 hi / lo parts of the sorted points
+  inca::DevBuf<int64_t> d_perm;       // sorted position -> grid index
+  inca::DevBuf<float> d_wtbox;        // per 128-point warp tile: lo[3], hi[3], 2 pad
 
   // scratch
   inca::DevBuf<double> d_partial;
   inca::DevBuf<unsigned char> d_scratch;
 
   // timing and tier statistics of the last evaluation
-  double t_total_ms = 0, t_kernel_ms = 0;
+  double t_total_ms = 0, t_kernel_ms = 0, t_pass2_ms = 0;
   int t_kernel_launches = 0, t_launches = 0;
   int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0;
   int64_t launches = 0;  // own kernel launches since creation

@@ -102,7 +102,7 @@ int eval_device(inca_ctx* c, int mode, double tol) {
   if (!c->prepared) return set_error(c, INCA_E_STATE, "inca_eval: call inca_prepare first");
   if (c->grid_kind == GRID_NONE || c->ngrid <= 0) return set_error(c, INCA_E_STATE, "inca_eval: no grid");
   if (c->d_ivec.reserve(c->ngrid)) return set_error(c, INCA_E_NOMEM, "ivec");
-  c->t_total_ms = c->t_kernel_ms = 0;
+  c->t_total_ms = c->t_kernel_ms = c->t_pass2_ms = 0;
   c->t_kernel_launches = c->t_launches = 0;
   c->pairs_fp32 = c->pairs_fp64 = c->pairs_skip = 0;
   if (mode == INCA_MIXED) {

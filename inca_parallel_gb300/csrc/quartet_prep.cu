@@ -279,7 +279,7 @@ __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl,
 // Pass 2: rebuild each survivor (identical arithmetic) and write its records into the
 // class segments:
 //   FP64 record [A, sqe, d0, d1, d2, A', Cx.., Cy.., Cz..] (C highest degree first);
-//   FP32 record [s_hi, s_lo, b_hi[3], b_lo[3], A'_hi, A'_lo, la, 0, Cn_x.., Cn_y.., Cn_z..]
+//   FP32 record [s_hi, s_lo, b_hi[3], b_lo[3], A'_hi, A'_lo, la, 0, Cn_hi (x,y,z), Cn_lo (x,y,z)]
 // with s = sqe c_u, b_d = s d_d, u = s (r + d) = c_u r', the polynomials rewritten in u and
 // scaled by kappa_d (largest |coefficient|) so that Cn has max |coefficient| 1, A' = A prod
 // kappa_d, and la = log2(|A'| prod_d sum_k |Cn_dk|). hi/lo pairs carry the FP64 value to
@@ -352,10 +352,17 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
   }
   r32[10] = static_cast<float>(la);
   r32[11] = 0.0f;
+  const int nc = rec.L[0] + rec.L[1] + rec.L[2] + 3;
   o = 12;
   for (int d = 0; d < 3; ++d)
-    for (int m = 0; m <= rec.L[d]; ++m) r32[o++] = static_cast<float>(Cu[d][m] / kappa[d]);
-  for (; o < sg.stride32; ++o) r32[o] = 0.0f;
+    for (int m = 0; m <= rec.L[d]; ++m) {
+      const double cn = Cu[d][m] / kappa[d];
+      const float hi = static_cast<float>(cn);
+      r32[o] = hi;
+      r32[o + nc] = static_cast<float>(cn - static_cast<double>(hi));
+      ++o;
+    }
+  for (o += nc; o < sg.stride32; ++o) r32[o] = 0.0f;
 }
 
 }  // namespace
@@ -473,7 +480,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     s.L[2] = hk[r] & 31;
     const int nc = s.L[0] + s.L[1] + s.L[2] + 3;
     s.stride = (kRecHeader + nc + 1) & ~1;
-    s.stride32 = (12 + nc + 3) & ~3;
+    s.stride32 = (12 + 2 * nc + 3) & ~3;
     s.first = nsurv;
     s.count = hcnt[r];
     s.off64 = off64;

@@ -157,11 +157,15 @@ int inca_centercalc(int32_t natoms, const int32_t* an, const double* cartes, int
 int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
                           int32_t* kernel_launches, int32_t* launches);
 
-/* Work split of the last INCA_MIXED evaluation, in (quartet, point tile) pairs: evaluated in
- * FP32, evaluated in FP64 (precise tier), skipped (bounded below the tolerance). The FP64
- * form reports zeros. Pointers may be NULL. */
-int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* fp64_pairs,
+/* Work split of the last INCA_MIXED evaluation, in (quartet, 128-point tile) pairs: kept in
+ * FP32, corrected in double-float arithmetic (the precise tier), skipped (bound below 2^-120).
+ * The FP64 form reports zeros. Pointers may be NULL. */
+int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* precise_pairs,
                          int64_t* skipped_pairs);
+
+/* Device milliseconds of the two passes of the last INCA_MIXED evaluation (estimate pass over
+ * all terms; correction pass). The FP64 form reports its single kernel as pass 1. */
+int inca_last_eval_phases(inca_ctx* ctx, double* pass1_ms, double* pass2_ms);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work or
  * record CUDA events around the library's calls. */

@@ -383,7 +383,7 @@ inline void accumulate(const Quartet& Q, long ngrid, const double* r, double* Iv
 
 // Becke/TFVC partition weights (mod_build_grid.f90:474-575).
 double tfvc_fk(double v) {
-  for (int i = 0; i < 4; ++i) v = 1.5 * v - 0.5 * std::pow(v, 3.0);
+  for (int i = 0; i < 4; ++i) v = 1.5 * v - 0.5 * ((v * v) * v);  // pf: 1.5 v - 0.5 v**3
   return v;
 }
 

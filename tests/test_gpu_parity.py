@@ -2,7 +2,7 @@
 
 Tolerances (written here, per the precision contract of the hot path):
   * screening values, flags and survivor records: bit-identical to the oracle;
-  * grids: 1e-14 relative (same formulas, different summation order in TFVC);
+  * grids: bit-identical (same operation sequence, no FMA contraction on either side);
   * FP64 form: 1e-12 relative to the oracle (summation order only);
   * mixed form: 1e-10 relative on the radial integral, 1e-8 relative on each I(s),
     1e-8 of max|I| on the vector cube, 1e-8 relative at explicit points.
@@ -60,9 +60,9 @@ def test_radial_grid_matches_oracle(ch4_ctx, ch4):
     g = O.gridpoints([50], [110], alf, cent, Ps)
     assert (mg, rg, ng) == (g["maxgrid"], g["rgrid"], len(g["w"]))
     mine = ctx.grid_copy(weights=True, vee=True, cmap=True)
-    np.testing.assert_allclose(mine["r"], g["r"], rtol=1e-15, atol=1e-15)
-    np.testing.assert_allclose(mine["w"], g["w"], rtol=1e-14)
-    np.testing.assert_allclose(mine["wvee"], g["wvee"], rtol=1e-14)
+    np.testing.assert_array_equal(mine["r"], g["r"])
+    np.testing.assert_array_equal(mine["w"], g["w"])
+    np.testing.assert_array_equal(mine["wvee"], g["wvee"])
     np.testing.assert_array_equal(mine["cmap"], g["cmap"] + 1)
 
 
@@ -75,8 +75,8 @@ def test_multicentre_grid_matches_oracle(ctx):
         g = O.gridpoints([40] * 5, [110, 110, 146, 110, 146], alf, cent, Ps, nosym=nosym)
         assert (mg, rg, ng) == (g["maxgrid"], g["rgrid"], len(g["w"]))
         mine = ctx.grid_copy(weights=True, vee=True, cmap=True)
-        np.testing.assert_allclose(mine["r"], g["r"], rtol=1e-15, atol=1e-15)
-        np.testing.assert_allclose(mine["w"], g["w"], rtol=1e-13, atol=1e-300)
+        np.testing.assert_array_equal(mine["r"], g["r"])
+        np.testing.assert_array_equal(mine["w"], g["w"])
         np.testing.assert_array_equal(mine["cmap"], g["cmap"] + 1)
 
 
