@@ -53,7 +53,7 @@ SIGNATURES = {
     "inca_radial_smearing": (ctypes.c_int, [VP, ctypes.c_double, ctypes.c_int32, ctypes.c_double, DP, DP, DP]),
     "inca_centercalc": (ctypes.c_int, [ctypes.c_int32, IP, DP, ctypes.c_int, ctypes.c_int, IP, DP, DP, DP]),
     "inca_last_eval_timing": (ctypes.c_int, [VP, DP, DP, IP, IP]),
-    "inca_last_eval_stats": (ctypes.c_int, [VP, I64P, I64P, I64P]),
+    "inca_last_eval_stats": (ctypes.c_int, [VP, I64P, I64P, I64P, I64P]),
     "inca_get_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
@@ -270,9 +270,10 @@ class Context:
         return n.value
 
     def stats(self):
-        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        self._check(self.lib.inca_last_eval_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value}
+        a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.inca_last_eval_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                  ctypes.byref(d)))
+        return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value, "corrected_terms": d.value}
 
     def phases(self):
         a, b = ctypes.c_double(), ctypes.c_double()

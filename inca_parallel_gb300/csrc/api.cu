@@ -363,11 +363,13 @@ int inca_last_eval_timing(inca_ctx* c, double* total_ms, double* kernel_ms, int3
   return INCA_OK;
 }
 
-int inca_last_eval_stats(inca_ctx* c, int64_t* fp32_pairs, int64_t* fp64_pairs, int64_t* skipped_pairs) {
+int inca_last_eval_stats(inca_ctx* c, int64_t* fp32_pairs, int64_t* precise_pairs, int64_t* skipped_pairs,
+                         int64_t* corrected_terms) {
   if (!c) return INCA_E_ARG;
   if (fp32_pairs) *fp32_pairs = c->pairs_fp32;
-  if (fp64_pairs) *fp64_pairs = c->pairs_fp64;
+  if (precise_pairs) *precise_pairs = c->pairs_fp64;
   if (skipped_pairs) *skipped_pairs = c->pairs_skip;
+  if (corrected_terms) *corrected_terms = c->corrected_points;
   return INCA_OK;
 }
 

@@ -1,7 +1,7 @@
 // K2 (mixed): FP32 evaluation with exact accumulation, plus a double-float correction of the
 // terms whose FP32 error could exceed the requested tolerance. Everything runs on the FP32
-// pipe (GB300's FP64 rate is ~1/64 of it); accumulation per point is exact (TwoSum in FP32
-// within a chunk of <= 32 quartets, then FP64 across chunks).
+// pipe (GB300's FP64 rate is ~1/64 of it); accumulation per point is exact (TwoSum in FP32,
+// moved to FP64 every few chunks).
 //
 // Why a correction. A term evaluated in FP32 carries ~2^-24 relative rounding; on a grid those
 // errors average only over the few terms that dominate each output, and symmetry-equivalent
@@ -9,23 +9,30 @@
 // relative on the CH4 radial integral. The large terms are therefore re-evaluated in
 // double-float arithmetic (~2^-44) and the difference is added.
 //
-// Points are evaluated in Morton order (a sorted copy of the grid), so the 128 points a warp
-// owns (32 lanes x 4) form a compact tile with a tight bounding box.
+// Work layout. Points are evaluated in Morton order (a sorted copy of the grid). A CTA is one
+// warp owning 128 consecutive points (4 per lane, 32-point sub-tiles p = lane + 32 k), each a
+// compact region with a bounding box. The CTA walks a strided subset of the class-uniform
+// chunks (<= 32 quartet records of one angular class); each chunk is staged into shared memory
+// by a 1-D TMA bulk copy (cp.async.bulk + mbarrier), double-buffered so the next chunk's copy
+// overlaps the current chunk's arithmetic. All waits are bounded; a wait that gives up sets an
+// error word that the host turns into INCA_E_TIMEOUT.
 //
 // Pass 1 (k_pass1): every (quartet, point) term in FP32 (compensated: hi/lo splits of the
-//   scale, the shift and the point), accumulated exactly; also sum |t| per point. Pairs whose
-//   bound is below 2^-120 (under FP32's normal range) are skipped.
+//   scale, the shift and the point), accumulated exactly; also the sum per point of e_t, a
+//   bound on each term's FP32 rounding error (see terms32). Pairs whose bound is below 2^-120
+//   (under FP32's normal range) are skipped.
 // Thresholds: for an output O = sum_g w_g I_g (radial integral: TFVC weights; I(s): angular
 //   weights of the shell; cube: max-norm; explicit points: each point) with tolerance eps,
-//   FP32 errors behave as independent kappa*u*|t| (u = 2^-24, kappa = 8), so keeping every
-//   uncorrected term below tau_g = (eps |O| / (3 kappa u))^2 / (w_g M_O) bounds the 3-sigma
-//   error by eps |O| / 3 (M_O = sum_g w_g sum_q |t_qg|). |O| is replaced by the lower bound
-//   |O~| - 3 kappa u M_O of the estimate.
-// Pass 2 (k_pass2): per (quartet, warp tile) the log2 upper bound
+//   the rounding errors of the uncorrected terms are independent, unbiased and bounded by e_t
+//   (variance <= e_t^2 / 3), so correcting every term with e_t > tau_g =
+//   (eps |O|)^2 / (3 w_g E_O) keeps 3 sigma of their sum (variance <= tau_g E_O / 3) below
+//   eps |O| (E_O = sum_g w_g sum_q e_qg). |O| is replaced by the lower bound |O~| - E_O.
+// Pass 2 (k_pass2): per (quartet, 32-point sub-tile) the log2 upper bound
 //   lb = log2(|A'| prod_d sum_k |Cn_dk|) + sum_d [L_d log2 max(1, M_d) - m_d^2]
-//   (m_d/M_d: min/max |u_d| over the tile's box, u = c_u r', e^-r'^2 = 2^-u^2) selects the
-//   pairs with lb > log2 tau_T; for those every point gets t_df - t_32, with t_32 recomputed by
-//   the same instruction sequence as in pass 1.
+//   (m_d/M_d: min/max |u_d| over the sub-tile's box, u = c_u r', e^-r'^2 = 2^-u^2), turned into
+//   a bound of e_t, selects the sub-tiles that may need a correction; there, every point with
+//   e_t > tau_g gets t_df - t_32 (t_32 recomputed by the same instruction sequence as in
+//   pass 1).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -41,94 +48,252 @@ int choose_splits(int64_t tiles, int64_t nchunks, int num_sms, int ctas_per_sm);
 
 namespace {
 
-constexpr int kWarps = 4;
-constexpr int kThreadsM = 32 * kWarps;
-constexpr int kPPT = 4;                        // points per lane
-constexpr int kWarpTile = 32 * kPPT;           // 128 points
-constexpr int kCtaTile = kWarps * kWarpTile;   // 512 points
+constexpr int kPPT = 4;                 // points per lane
+constexpr int kWarpTile = 32 * kPPT;    // 128 points per CTA (one warp)
 constexpr int kMaxStride32 = (12 + 2 * 3 * kMaxCoef + 3) & ~3;
 constexpr int kChunkMax = 32;
-constexpr double kKappaU = 8.0 * 5.9604644775390625e-08;  // kappa * 2^-24
-constexpr float kSkipLog2 = -120.0f;                      // pass-1 skip: bound below 2^-120
-constexpr int kExpTab = 256;                              // 2^(j/256), j = -128..128
+// tau = kTauScale (eps |O|)^2 / E_O: the error of an uncorrected term is a sum of independent
+// round-to-nearest errors bounded in total by e_t, so its variance is <= e_t^2 / 3, and
+// 3 sigma <= eps |O| gives tau <= 3 (eps |O| / 3)^2 / E_O.
+constexpr double kTauScale = 1.0 / 3.0;
+constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
+constexpr int kExpTab = 256;             // 2^(j/256), j = -128..128
+constexpr int kFold = 8;                 // chunks between FP64 folds
+constexpr int kWaitLimit = 1 << 22;      // bounded mbarrier waits
 
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
+// 2^y for y <= 0 in FP32 without systematic bias: y = n + f (n = rint(y), |f| <= 1/2),
+// 2^f by a degree-7 polynomial (Chebyshev interpolation of 2^x on [-1/2, 1/2], relative
+// approximation error 3.2e-9) evaluated by FMA Horner (<= 1.1 ulp), times 2^n built from the
+// exponent bits (exact; 0 below 2^-126). The hardware ex2.approx was measured biased by
+// -5e-8 relative on this range, which the error model of the correction pass cannot absorb.
+__device__ __forceinline__ float exp2_fp32(float y) {
+  const float n = rintf(y);
+  const float f = __fsub_rn(y, n);
+  float p = 1.5303699910873547e-05f;
+  p = __fmaf_rn(p, f, 0.00015469729260075837f);
+  p = __fmaf_rn(p, f, 0.0013333478709682822f);
+  p = __fmaf_rn(p, f, 0.00961802527308464f);
+  p = __fmaf_rn(p, f, 0.05550410971045494f);
+  p = __fmaf_rn(p, f, 0.24022650718688965f);
+  p = __fmaf_rn(p, f, 0.6931471824645996f);
+  p = __fmaf_rn(p, f, 1.0f);
+  const int e = max(static_cast<int>(n) + 127, 0);
+  return __fmul_rn(p, __int_as_float(e << 23));
+}
+
+// ---------------------------------------------------------------- TMA bulk staging
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// One thread: expect `bytes` on the barrier and start the bulk copy global -> shared.
+// Requires 16-byte aligned addresses and a size that is a multiple of 16.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Bounded wait for the barrier phase with the given parity; false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+struct ChunkRef {
+  const float* src;
+  uint32_t bytes;
+};
+__device__ __forceinline__ ChunkRef chunk_ref(const WorkChunk* chunks, const ClassSeg* segs, const float* rec32,
+                                              int ch) {
+  const WorkChunk w = chunks[ch];
+  const ClassSeg sg = segs[w.cls];
+  return {rec32 + sg.off32 + (w.rec - sg.first) * sg.stride32,
+          static_cast<uint32_t>(w.count * sg.stride32 * sizeof(float))};
 }
 
 // ---------------------------------------------------------------- FP32 term (both passes)
-template <int L>
-__device__ __forceinline__ void horner_pts(const float* __restrict__ C, const float (&u)[kPPT], float (&v)[kPPT]) {
+template <int NP, int L>
+__device__ __forceinline__ void horner_pts(const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) v[p] = C[0];
+  for (int p = 0; p < NP; ++p) v[p] = C[0];
 #pragma unroll
   for (int m = 1; m <= L; ++m) {
     const float c = C[m];
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) v[p] = __fmaf_rn(v[p], u[p], c);
+    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], u[p], c);
   }
 }
 
-__device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, const float (&u)[kPPT], float (&v)[kPPT]) {
+template <int NP, int L>
+__device__ __forceinline__ void horner_abs_pts(const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
+#pragma unroll
+  for (int p = 0; p < NP; ++p) v[p] = fabsf(C[0]);
+#pragma unroll
+  for (int m = 1; m <= L; ++m) {
+    const float c = fabsf(C[m]);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], fabsf(u[p]), c);
+  }
+}
+
+// Polynomial of a class-uniform (warp-uniform) degree: one indirect branch per quartet.
+// kAbs: sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error.
+template <int NP, bool kAbs>
+__device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
+#define INCA_POLY_CASE(n)                      \
+  case n:                                      \
+    if (kAbs) horner_abs_pts<NP, n>(C, u, v);  \
+    else horner_pts<NP, n>(C, u, v);           \
+    break;
   switch (L) {
-    case 0: horner_pts<0>(C, u, v); break;
-    case 1: horner_pts<1>(C, u, v); break;
-    case 2: horner_pts<2>(C, u, v); break;
-    case 3: horner_pts<3>(C, u, v); break;
-    case 4: horner_pts<4>(C, u, v); break;
-    case 5: horner_pts<5>(C, u, v); break;
-    case 6: horner_pts<6>(C, u, v); break;
-    case 7: horner_pts<7>(C, u, v); break;
-    case 8: horner_pts<8>(C, u, v); break;
-    case 9: horner_pts<9>(C, u, v); break;
-    case 10: horner_pts<10>(C, u, v); break;
-    case 11: horner_pts<11>(C, u, v); break;
-    case 12: horner_pts<12>(C, u, v); break;
-    case 13: horner_pts<13>(C, u, v); break;
-    case 14: horner_pts<14>(C, u, v); break;
-    case 15: horner_pts<15>(C, u, v); break;
-    default: horner_pts<16>(C, u, v); break;
+    INCA_POLY_CASE(0) INCA_POLY_CASE(1) INCA_POLY_CASE(2) INCA_POLY_CASE(3) INCA_POLY_CASE(4)
+    INCA_POLY_CASE(5) INCA_POLY_CASE(6) INCA_POLY_CASE(7) INCA_POLY_CASE(8) INCA_POLY_CASE(9)
+    INCA_POLY_CASE(10) INCA_POLY_CASE(11) INCA_POLY_CASE(12) INCA_POLY_CASE(13) INCA_POLY_CASE(14)
+    INCA_POLY_CASE(15)
+    default:
+      if (kAbs) horner_abs_pts<NP, 16>(C, u, v);
+      else horner_pts<NP, 16>(C, u, v);
+      break;
   }
+#undef INCA_POLY_CASE
 }
 
-// The FP32 term of quartet record R at kPPT points. Explicit round-to-nearest intrinsics only,
-// so both passes produce the same bits.
-__device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][kPPT],
-                                        const float (&rl)[3][kPPT], float (&t)[kPPT]) {
+// The FP32 term of quartet record R at NP points, and a bound e on its rounding error:
+//   u_d = fma(s_hi, r_hi, b_hi) + [s_hi r_lo + s_lo r_hi + b_lo]  (error <= u32 |u_d|)
+//   y = -|u|^2 (error <= 4 u32 |y| with the u errors), E = exp2_fp32(y) (<= 2 u32)
+//   V_d by Horner (absolute error <= 2 L_d u32 P_d, P_d = sum_k |C_k| |u_d|^k), 4 products
+//   e = u32 |A'| E prod_d P_d (10 + 2 L + 3 |y|).
+// Explicit round-to-nearest intrinsics only, so both passes produce the same bits.
+template <int NP, bool kErr>
+__device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
+                                        const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
   const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
-  float u[3][kPPT];
+  float u[3][NP];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float b_hi = R[2 + d], b_lo = R[5 + d];
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) {
+    for (int p = 0; p < NP; ++p) {
       float t1 = __fmaf_rn(s_lo, rh[d][p], b_lo);
       t1 = __fmaf_rn(s_hi, rl[d][p], t1);
-      u[d][p] = __fmaf_rn(s_hi, rh[d][p], __fadd_rn(b_hi, t1));
+      u[d][p] = __fadd_rn(__fmaf_rn(s_hi, rh[d][p], b_hi), t1);
     }
   }
-  float E[kPPT];
+  float E[NP], Y[NP];
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
+  for (int p = 0; p < NP; ++p) {
     float y = __fmul_rn(-u[0][p], u[0][p]);
     y = __fmaf_rn(-u[1][p], u[1][p], y);
     y = __fmaf_rn(-u[2][p], u[2][p], y);
-    E[p] = ex2_approx(y);
+    Y[p] = y;
+    E[p] = exp2_fp32(y);
   }
   const float* Cx = R + 12;
   const float* Cy = Cx + L[0] + 1;
   const float* Cz = Cy + L[1] + 1;
-  float vx[kPPT], vy[kPPT], vz[kPPT];
-  poly_pts(L[0], Cx, u[0], vx);
-  poly_pts(L[1], Cy, u[1], vy);
-  poly_pts(L[2], Cz, u[2], vz);
+  // dimensions with L_d = 0 have V_d = 1 exactly (sign folded into A'): skipped
+  float P[NP];
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    const float P = __fmul_rn(__fmul_rn(__fmul_rn(E[p], vx[p]), vy[p]), vz[p]);
-    t[p] = __fmaf_rn(P, A_hi, __fmul_rn(P, A_lo));
+  for (int p = 0; p < NP; ++p) P[p] = E[p];
+  float v[NP];
+  if (L[0]) {
+    poly_pts<NP, false>(L[0], Cx, u[0], v);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
   }
+  if (L[1]) {
+    poly_pts<NP, false>(L[1], Cy, u[1], v);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
+  }
+  if (L[2]) {
+    poly_pts<NP, false>(L[2], Cz, u[2], v);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
+  }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(P[p], A_hi, __fmul_rn(P[p], A_lo));
+  if (kErr) {
+    const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
+    const float aA = 5.9604645e-08f * fabsf(A_hi);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(E[p], __fmaf_rn(fabsf(Y[p]), 3.0f * aA, k0 * fabsf(A_hi)));
+    if (L[0]) {
+      poly_pts<NP, true>(L[0], Cx, u[0], v);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
+    }
+    if (L[1]) {
+      poly_pts<NP, true>(L[1], Cy, u[1], v);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
+    }
+    if (L[2]) {
+      poly_pts<NP, true>(L[2], Cz, u[2], v);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) err[p] = P[p];
+  }
+}
+
+// The same FP32 term and error bound for one point with loop-based Horner (compact code for
+// the correction pass; same operation sequence and rounding as terms32).
+__device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry,
+                                        float rz, float lx, float ly, float lz, float* t_out, float* e_out) {
+  const int L[3] = {L0, L1, L2};
+  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
+  const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
+  float u[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float t1 = __fmaf_rn(s_lo, rh[d], R[5 + d]);
+    t1 = __fmaf_rn(s_hi, rl[d], t1);
+    u[d] = __fadd_rn(__fmaf_rn(s_hi, rh[d], R[2 + d]), t1);
+  }
+  float y = __fmul_rn(-u[0], u[0]);
+  y = __fmaf_rn(-u[1], u[1], y);
+  y = __fmaf_rn(-u[2], u[2], y);
+  const float E = exp2_fp32(y);
+  const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L0 + L1 + L2));
+  const float aA = 5.9604645e-08f * fabsf(A_hi);
+  float P = E, Pe = __fmul_rn(E, __fmaf_rn(fabsf(y), 3.0f * aA, k0 * fabsf(A_hi)));
+  const float* C = R + 12;
+  for (int d = 0; d < 3; ++d) {
+    if (L[d]) {
+      float v = C[0], va = fabsf(C[0]);
+      for (int m = 1; m <= L[d]; ++m) {
+        v = __fmaf_rn(v, u[d], C[m]);
+        va = __fmaf_rn(va, fabsf(u[d]), fabsf(C[m]));
+      }
+      P = __fmul_rn(P, v);
+      Pe = __fmul_rn(Pe, va);
+    }
+    C += L[d] + 1;
+  }
+  *t_out = __fmaf_rn(P, A_hi, __fmul_rn(P, A_lo));
+  *e_out = Pe;
 }
 
 // ---------------------------------------------------------------- double-float arithmetic
@@ -168,7 +333,7 @@ __device__ __forceinline__ f2 df_sqr(f2 x) {
 __device__ __forceinline__ f2 df_exp2(f2 y, const float2* __restrict__ tab) {
   if (y.hi < -125.0f) return {0.0f, 0.0f};
   const float n = rintf(y.hi);
-  const float f = __fsub_rn(y.hi, n);           // exact
+  const float f = __fsub_rn(y.hi, n);  // exact
   const float j = rintf(__fmul_rn(f, 256.0f));
   const float g = __fsub_rn(f, __fmul_rn(j, 0.00390625f));  // exact
   const float kLn2Hi = 0.693147182464599609375f, kLn2Lo = -1.904654323148236e-09f;
@@ -190,8 +355,11 @@ __device__ __forceinline__ f2 df_exp2(f2 y, const float2* __restrict__ tab) {
 }
 
 // The double-float term of record R at one point (r_hi + r_lo per dimension).
-__device__ f2 term_df(const float* __restrict__ R, const int L[3], int nc, const float rh[3], const float rl[3],
-                      const float2* __restrict__ tab) {
+__device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry, float rz,
+                                   float lx, float ly, float lz, const float2* __restrict__ tab) {
+  const int L[3] = {L0, L1, L2};
+  const int nc = L0 + L1 + L2 + 3;
+  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
   const float s_hi = R[0], s_lo = R[1];
   f2 u[3];
 #pragma unroll
@@ -203,7 +371,7 @@ __device__ f2 term_df(const float* __restrict__ R, const int L[3], int nc, const
     e = __fmaf_rn(s_hi, rl[d], e);
     e = __fmaf_rn(s_lo, rh[d], e);
     e = __fadd_rn(e, R[5 + d]);
-    u[d] = two_sum(t.hi, e);
+    u[d] = fast_two_sum(t.hi, e);  // |e| << |t.hi| except near u = 0, where it is harmless
   }
   f2 y = df_add(df_add(df_sqr(u[0]), df_sqr(u[1])), df_sqr(u[2]));
   y.hi = -y.hi;
@@ -213,6 +381,11 @@ __device__ f2 term_df(const float* __restrict__ R, const int L[3], int nc, const
   int o = 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
+    if (L[d] == 0) {  // normalised constant polynomial: exactly +-1
+      if (C[o] < 0.0f) t = {-t.hi, -t.lo};
+      o += 1;
+      continue;
+    }
     f2 v = {C[o], C[o + nc]};
     for (int m = 1; m <= L[d]; ++m) v = df_add(df_mul(v, u[d]), f2{C[o + m], C[o + m + nc]});
     o += L[d] + 1;
@@ -221,9 +394,12 @@ __device__ f2 term_df(const float* __restrict__ R, const int L[3], int nc, const
   return df_mul(t, f2{R[8], R[9]});
 }
 
-// log2 upper bound of |term| over a tile's box (see the file comment).
-__device__ __forceinline__ float log2_bound(const float* __restrict__ R, const int L[3], const float box[6]) {
+// log2 upper bound of |A'| E prod_d P_d over a box (see the file comment); *lerr gets the log2
+// bound of the FP32 error bound e over the box.
+__device__ __forceinline__ float log2_bound(const float* __restrict__ R, const int L[3], const float* box,
+                                           float* lerr = nullptr) {
   float lb = R[10] + 0.02f;
+  float y2 = 0.0f;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float s = R[0], b = R[2 + d];
@@ -233,7 +409,9 @@ __device__ __forceinline__ float log2_bound(const float* __restrict__ R, const i
     m = fmaxf(0.0f, m * (1.0f - 1e-5f) - 1e-5f);
     M = M * (1.0f + 1e-5f) + 1e-5f;
     lb += static_cast<float>(L[d]) * __log2f(fmaxf(M, 1.0f)) - m * m;
+    y2 = fmaf(M, M, y2);
   }
+  if (lerr) *lerr = lb - 24.0f + __log2f(static_cast<float>(10 + 2 * (L[0] + L[1] + L[2])) + 3.0f * y2) + 0.02f;
   return lb;
 }
 
@@ -253,143 +431,231 @@ __device__ __forceinline__ void load_points(const float4* __restrict__ phi, cons
   }
 }
 
-__device__ __forceinline__ void stage_chunk(float* st, const float* __restrict__ rec32, const ClassSeg& sg,
-                                            const WorkChunk& w) {
-  const float4* src = reinterpret_cast<const float4*>(rec32 + sg.off32 + (w.rec - sg.first) * sg.stride32);
-  const int nvec = w.count * sg.stride32 / 4;
-  for (int i = threadIdx.x; i < nvec; i += kThreadsM) reinterpret_cast<float4*>(st)[i] = src[i];
+// Shared-memory stage of a warp-CTA (dynamic shared memory): two barriers, then two chunk
+// buffers of `floats` floats each (32 records of the largest stride present).
+struct Stage {
+  uint64_t* bar;
+  float* buf[2];
+};
+__device__ __forceinline__ Stage stage_view(unsigned char* dsm, int floats) {
+  Stage S;
+  S.bar = reinterpret_cast<uint64_t*>(dsm);
+  S.buf[0] = reinterpret_cast<float*>(dsm + 128);
+  S.buf[1] = S.buf[0] + floats;
+  return S;
+}
+
+// Set up the barriers and start the first chunk's copy (lane 0).
+__device__ __forceinline__ void stage_begin(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
+                                            const float* rec32, int first, int nchunks) {
+  if (threadIdx.x == 0) {
+    mbar_init(&S.bar[0]);
+    mbar_init(&S.bar[1]);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  if (threadIdx.x == 0 && first < nchunks) {
+    const ChunkRef r = chunk_ref(chunks, segs, rec32, first);
+    bulk_load(S.buf[0], r.src, r.bytes, &S.bar[0]);
+  }
+}
+
+// Before working on chunk k: start the copy of the next chunk into the other buffer, then wait
+// for this one. Returns false if the wait gave up; the other buffer's copy (if started) is then
+// drained, again with a bounded wait, so no copy is left in flight when the CTA exits.
+__device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
+                                           const float* rec32, int k, int next, int nchunks) {
+  if (threadIdx.x == 0 && next < nchunks) {
+    fence_proxy_async();  // the generic-proxy reads of that buffer (chunk k-1) are done
+    const ChunkRef r = chunk_ref(chunks, segs, rec32, next);
+    bulk_load(S.buf[(k + 1) & 1], r.src, r.bytes, &S.bar[(k + 1) & 1]);
+  }
+  if (mbar_wait(&S.bar[k & 1], static_cast<uint32_t>((k >> 1) & 1))) return true;
+  if (next < nchunks) mbar_wait(&S.bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1));
+  return false;
 }
 
 // ---------------------------------------------------------------- pass 1
-__global__ void __launch_bounds__(kThreadsM)
+__global__ void __launch_bounds__(32, 16)
 k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
-        const float* __restrict__ wtbox, int64_t ngrid, int nsplit, double* __restrict__ part,
-        double* __restrict__ part_abs, unsigned long long* __restrict__ stats) {
-  __shared__ __align__(16) float st[kChunkMax * kMaxStride32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t wtile = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
+        const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part,
+        double* __restrict__ part_abs, unsigned long long* __restrict__ stats, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char dsm[];
+  const Stage S = stage_view(dsm, stage_floats);
+  const int lane = threadIdx.x;
+  const int64_t wtile = blockIdx.x;
   const int64_t base = wtile * kWarpTile;
+  stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
   float rh[3][kPPT], rl[3][kPPT];
   load_points(phi, plo, base, lane, ngrid, rh, rl);
   float box[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) box[k] = wtbox[wtile * 8 + k];
-  double acc[kPPT], acc_abs[kPPT];
+  double acc[kPPT];
+  float sh[kPPT], sl[kPPT], sa[kPPT];
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) acc[p] = acc_abs[p] = 0.0;
+  for (int p = 0; p < kPPT; ++p) {
+    acc[p] = 0.0;
+    sh[p] = sl[p] = sa[p] = 0.0f;
+  }
   unsigned long long nskip = 0;
-  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit) {
+  int nfold = 0, k = 0;
+  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit, ++k) {
+    if (!stage_next(S, chunks, segs, rec32, k, ch + nsplit, nchunks)) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
     const WorkChunk w = chunks[ch];
     const ClassSeg sg = segs[w.cls];
-    __syncthreads();
-    stage_chunk(st, rec32, sg, w);
-    __syncthreads();
+    const float* st = S.buf[k & 1];
     const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
     const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
     uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > kSkipLog2);
     if (lane == 0) nskip += w.count - __popc(m);
-    float sh[kPPT], sl[kPPT], sa[kPPT];
-#pragma unroll
-    for (int p = 0; p < kPPT; ++p) sh[p] = sl[p] = sa[p] = 0.0f;
     while (m) {
       const int q = __ffs(m) - 1;
       m &= m - 1;
-      float t[kPPT];
-      terms32(st + q * sg.stride32, L, rh, rl, t);
+      float t[kPPT], e[kPPT];
+      terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         const f2 s = two_sum(sh[p], t[p]);
         sh[p] = s.hi;
         sl[p] = __fadd_rn(sl[p], s.lo);
-        sa[p] = __fadd_rn(sa[p], fabsf(t[p]));
+        sa[p] = __fadd_rn(sa[p], e[p]);
       }
     }
+    // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
+    const bool fold = ++nfold == kFold;
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
-      acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
-      acc_abs[p] += static_cast<double>(sa[p]);
+      const f2 r = fast_two_sum(sh[p], sl[p]);
+      sh[p] = r.hi;
+      sl[p] = r.lo;
+      if (fold) {
+        acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
+        sh[p] = sl[p] = 0.0f;
+      }
     }
+    if (fold) nfold = 0;
+    __syncwarp();
   }
 #pragma unroll
   for (int p = 0; p < kPPT; ++p) {
+    acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
     const int64_t i = base + lane + 32 * p;
     if (i < ngrid) {
       part[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc[p];
-      part_abs[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc_abs[p];
+      part_abs[static_cast<int64_t>(blockIdx.y) * ngrid + i] = static_cast<double>(sa[p]);
     }
   }
   if (lane == 0) atomicAdd(&stats[2], nskip);
 }
 
 // ---------------------------------------------------------------- pass 2 (corrections)
-__global__ void __launch_bounds__(kThreadsM)
+__global__ void __launch_bounds__(32, 16)
 k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
-        const float* __restrict__ wtbox, const float* __restrict__ wt_lt, const float2* __restrict__ exp_tab,
-        int64_t ngrid, int nsplit, double* __restrict__ part, unsigned long long* __restrict__ stats) {
-  __shared__ __align__(16) float st[kChunkMax * kMaxStride32];
+        const float* __restrict__ wtbox, const float* __restrict__ gbox, const float* __restrict__ g_lt,
+        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, int64_t ngrid, int nsplit,
+        int stage_floats, double* __restrict__ part, unsigned long long* __restrict__ stats, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char dsm[];
+  const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kExpTab + 1];
-  for (int i = threadIdx.x; i <= kExpTab; i += kThreadsM) tab[i] = exp_tab[i];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t wtile = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
+  const int lane = threadIdx.x;
+  const int64_t wtile = blockIdx.x;
   const int64_t base = wtile * kWarpTile;
-  float rh[3][kPPT], rl[3][kPPT];
+  stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
+  for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
+  float rh[3][kPPT], rl[3][kPPT], tau[kPPT];
   load_points(phi, plo, base, lane, ngrid, rh, rl);
-  float box[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) box[k] = wtbox[wtile * 8 + k];
-  const float lt = wt_lt[wtile];
+  for (int p = 0; p < kPPT; ++p) {
+    const int64_t i = base + lane + 32 * p;
+    tau[p] = i < ngrid ? pt_tau[i] : HUGE_VALF;
+  }
+  float wbox[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) wbox[k] = wtbox[wtile * 8 + k];
   double acc[kPPT];
+  f2 corr[kPPT];
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) acc[p] = 0.0;
-  unsigned long long n32 = 0, ndf = 0;
-  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit) {
+  for (int p = 0; p < kPPT; ++p) {
+    acc[p] = 0.0;
+    corr[p] = {0.0f, 0.0f};
+  }
+  __syncwarp();
+  unsigned long long n32 = 0, ndf = 0, npts = 0;
+  int nfold = 0, k = 0;
+  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit, ++k) {
+    if (!stage_next(S, chunks, segs, rec32, k, ch + nsplit, nchunks)) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
     const WorkChunk w = chunks[ch];
     const ClassSeg sg = segs[w.cls];
-    __syncthreads();
-    stage_chunk(st, rec32, sg, w);
-    __syncthreads();
+    const float* st = S.buf[k & 1];
     const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
-    const int nc = L[0] + L[1] + L[2] + 3;
-    const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
+    const float* Rq = st + lane * sg.stride32;
+    // pass 1's skip decision for this quartet (same box, same arithmetic)
+    const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
     const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > kSkipLog2);
-    uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > lt);
-    if (lane == 0) {
-      ndf += __popc(m);
-      n32 += __popc(live & ~m);
+    uint32_t msub[kPPT];
+    uint32_t any = 0;
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) {
+      float lerr = -HUGE_VALF;
+      if (lane < w.count) log2_bound(Rq, L, gbox + (wtile * kPPT + p) * 8, &lerr);
+      msub[p] = __ballot_sync(0xffffffffu, lane < w.count && lerr > g_lt[wtile * kPPT + p]);
+      any |= msub[p];
     }
-    if (!m) continue;
-    f2 corr[kPPT];
+    if (lane == 0) {
+      ndf += __popc(any);
+      n32 += __popc(live & ~any);
+    }
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) corr[p] = {0.0f, 0.0f};
-    while (m) {
-      const int q = __ffs(m) - 1;
-      m &= m - 1;
-      const float* R = st + q * sg.stride32;
-      float t32[kPPT];
-      terms32(R, L, rh, rl, t32);
-      const bool was_live = (live >> q) & 1u;
-#pragma unroll
-      for (int p = 0; p < kPPT; ++p) {
-        const float ph[3] = {rh[0][p], rh[1][p], rh[2][p]};
-        const float pl[3] = {rl[0][p], rl[1][p], rl[2][p]};
-        f2 tdf = term_df(R, L, nc, ph, pl, tab);
-        if (was_live) tdf = df_add(tdf, f2{-t32[p], 0.0f});
-        corr[p] = df_add(corr[p], tdf);
+    for (int p = 0; p < kPPT; ++p) {
+      uint32_t m = msub[p];
+      const float ph[3][1] = {{rh[0][p]}, {rh[1][p]}, {rh[2][p]}};
+      const float pl[3][1] = {{rl[0][p]}, {rl[1][p]}, {rl[2][p]}};
+      while (m) {
+        const int q = __ffs(m) - 1;
+        m &= m - 1;
+        const float* R = st + q * sg.stride32;
+        float t32[1], e32[1];
+        term32_one(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], t32, e32);
+        const bool need = e32[0] * 1.01f > tau[p];
+        if (__any_sync(0xffffffffu, need)) {
+          if (lane == 0) ++npts;
+          if (need) {
+            f2 tdf = term_df(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], tab);
+            if ((live >> q) & 1u) tdf = df_add(tdf, f2{-t32[0], 0.0f});
+            corr[p] = df_add(corr[p], tdf);
+          }
+        }
       }
     }
+    if (++nfold == kFold) {
+      nfold = 0;
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+      for (int p = 0; p < kPPT; ++p) {
+        acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+        corr[p] = {0.0f, 0.0f};
+      }
+    }
+    __syncwarp();
   }
 #pragma unroll
   for (int p = 0; p < kPPT; ++p) {
+    acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
     const int64_t i = base + lane + 32 * p;
     if (i < ngrid) part[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc[p];
   }
   if (lane == 0) {
     atomicAdd(&stats[0], n32);
     atomicAdd(&stats[1], ndf);
+    atomicAdd(&stats[3], npts);
   }
 }
 
@@ -425,63 +691,72 @@ __global__ void k_gather_points(int64_t n, const int64_t* __restrict__ perm, con
   plo[i] = make_float4(l[0], l[1], l[2], 0.0f);
 }
 
-// Bounding box of each 128-point warp tile (FP32, rounded outwards).
-__global__ void k_warp_boxes(int64_t n, int64_t nwt, const float4* __restrict__ phi, const float4* __restrict__ plo,
-                             float* box) {
+// Bounding boxes (FP32, rounded outwards) of each 128-point tile and its four 32-point
+// sub-tiles (points lane + 32 p). One warp per tile.
+__global__ void k_boxes(int64_t n, int64_t nwt, const float4* __restrict__ phi, const float4* __restrict__ plo,
+                        float* wbox, float* gbox) {
   const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (wt >= nwt) return;
   const int lane = threadIdx.x & 31;
-  float lo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF}, hi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
+  float tlo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF}, thi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
   for (int p = 0; p < kPPT; ++p) {
     const int64_t i = wt * kWarpTile + lane + 32 * p;
-    if (i >= n) break;
-    const float4 h = phi[i], l = plo[i];
-    const float x[3] = {h.x + l.x, h.y + l.y, h.z + l.z};
+    float lo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF}, hi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
+    if (i < n) {
+      const float4 h = phi[i], l = plo[i];
+      const float x[3] = {h.x + l.x, h.y + l.y, h.z + l.z};
+      for (int d = 0; d < 3; ++d) lo[d] = hi[d] = x[d];
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+        hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+      }
     for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], x[d]);
-      hi[d] = fmaxf(hi[d], x[d]);
+      const float l = lo[d] - (fabsf(lo[d]) * 1e-6f + 1e-6f), h = hi[d] + (fabsf(hi[d]) * 1e-6f + 1e-6f);
+      if (lane == 0) {
+        gbox[(wt * kPPT + p) * 8 + d] = l;
+        gbox[(wt * kPPT + p) * 8 + 3 + d] = h;
+      }
+      tlo[d] = fminf(tlo[d], l);
+      thi[d] = fmaxf(thi[d], h);
     }
   }
-  for (int o = 16; o > 0; o >>= 1)
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-    }
   if (lane == 0)
     for (int d = 0; d < 3; ++d) {
-      box[wt * 8 + d] = lo[d] - (fabsf(lo[d]) * 1e-6f + 1e-6f);
-      box[wt * 8 + 3 + d] = hi[d] + (fabsf(hi[d]) * 1e-6f + 1e-6f);
+      wbox[wt * 8 + d] = tlo[d];
+      wbox[wt * 8 + 3 + d] = thi[d];
     }
 }
 
-// Per-point thresholds (sorted order) reduced to per-warp-tile log2 minima.
-// mode 0: tau = T_o / w_g; mode 1 (max-norm): tau = T_o / M_g; mode 2 (per point).
-__global__ void k_warp_thresholds(int64_t n, int64_t nwt, int mode, const int64_t* __restrict__ perm,
-                                  const int* __restrict__ seg_of, const double* __restrict__ segT,
-                                  const double* __restrict__ w, const double* __restrict__ I,
-                                  const double* __restrict__ M, double eps, float* lt) {
-  const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
-  if (wt >= nwt) return;
+// Per-point thresholds tau_g (sorted order) and their minimum per 32-point sub-tile (log2).
+// mode 0: tau = T_o / w_g; mode 1 (max-norm): tau = T_o / E_g; mode 2 (per point).
+__global__ void k_thresholds(int64_t n, int64_t ngroups, int mode, const int64_t* __restrict__ perm,
+                             const int* __restrict__ seg_of, const double* __restrict__ segT,
+                             const double* __restrict__ w, const double* __restrict__ I,
+                             const double* __restrict__ M, double eps, float* g_lt, float* pt_tau) {
+  const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
+  if (grp >= ngroups) return;
   const int lane = threadIdx.x & 31;
-  double tmin = HUGE_VAL;
-  for (int p = 0; p < kPPT; ++p) {
-    const int64_t i = wt * kWarpTile + lane + 32 * p;
-    if (i >= n) break;
+  // group grp = tile grp / kPPT, sub-tile grp % kPPT: points tile*128 + lane + 32*sub
+  const int64_t i = (grp / kPPT) * kWarpTile + lane + 32 * (grp % kPPT);
+  double tau = HUGE_VAL;
+  if (i < n) {
     const int64_t g = perm[i];
-    double tau;
     if (mode == 0) {
       tau = w[g] > 0.0 ? segT[seg_of ? seg_of[g] : 0] / w[g] : HUGE_VAL;
     } else if (mode == 1) {
       tau = M[i] > 0.0 ? segT[0] / M[i] : HUGE_VAL;
     } else {
-      const double lo = fmax(fabs(I[i]) - 3.0 * kKappaU * M[i], 0.0);
-      const double x = eps * lo / (3.0 * kKappaU);
-      tau = M[i] > 0.0 ? x * x / M[i] : HUGE_VAL;
+      const double lo = fmax(fabs(I[i]) - M[i], 0.0);
+      const double x = eps * lo;
+      tau = M[i] > 0.0 ? kTauScale * x * x / M[i] : HUGE_VAL;
     }
-    tmin = fmin(tmin, tau);
+    pt_tau[i] = tau >= 3.0e38 ? HUGE_VALF : static_cast<float>(tau);
   }
+  double tmin = tau;
   for (int o = 16; o > 0; o >>= 1) tmin = fmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-  if (lane == 0) lt[wt] = tmin >= HUGE_VAL ? HUGE_VALF : (tmin > 0.0 ? static_cast<float>(log2(tmin)) : -HUGE_VALF);
+  if (lane == 0) g_lt[grp] = tmin >= HUGE_VAL ? HUGE_VALF : (tmin > 0.0 ? static_cast<float>(log2(tmin)) : -HUGE_VALF);
 }
 
 // Sum the split partials of the passes (sorted order) in a fixed order.
@@ -538,13 +813,13 @@ __global__ void k_absmax(int64_t n, const double* __restrict__ I, unsigned long 
 
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
-// Morton-sorted FP32 copy of the grid, the permutation and the warp-tile boxes.
+// Morton-sorted FP32 copy of the grid, the permutation and the tile / sub-tile boxes.
 int prepare_sorted_grid(inca_ctx* c) {
   if (c->mix_version == c->grid_version) return INCA_OK;
   const int64_t n = c->ngrid;
-  const int64_t ctas = (n + kCtaTile - 1) / kCtaTile;
-  const int64_t nwt = ctas * kWarps;
-  if (c->d_phi.reserve(n) || c->d_plo.reserve(n) || c->d_perm.reserve(n) || c->d_wtbox.reserve(8 * nwt))
+  const int64_t nwt = (n + kWarpTile - 1) / kWarpTile;
+  if (c->d_phi.reserve(n) || c->d_plo.reserve(n) || c->d_perm.reserve(n) ||
+      c->d_wtbox.reserve(8 * nwt + 8 * nwt * kPPT))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
   // bounding box of the grid (one host copy of the coordinates; cheap next to evaluation)
   std::vector<double> hx(n), hy(n), hz(n);
@@ -575,11 +850,8 @@ int prepare_sorted_grid(inca_ctx* c) {
   if (!e) {
     INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, c->d_perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_phi.p,
                 c->d_plo.p);
-    e = cudaMemsetAsync(c->d_wtbox.p, 0, sizeof(float) * 8 * nwt, c->stream);
-  }
-  if (!e) {
-    INCA_LAUNCH(c, k_warp_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, n, nwt, c->d_phi.p, c->d_plo.p,
-                c->d_wtbox.p);
+    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, n, nwt, c->d_phi.p, c->d_plo.p,
+                c->d_wtbox.p, c->d_wtbox.p + 8 * nwt);
     e = cudaStreamSynchronize(c->stream);
   }
   rel();
@@ -614,31 +886,41 @@ int eval_mixed(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaEventRecord(ev[0], c->stream));
   int st = prepare_sorted_grid(c);
   if (st) return st;
-  const int64_t ctas = (ngrid + kCtaTile - 1) / kCtaTile;
-  const int64_t nwt = ctas * kWarps;
-  const int nsplit = choose_splits(ctas, nchunks, c->num_sms, 4);
-  // scratch: pass-1 sums and |t| sums, pass-2 corrections (nsplit x n each), I~, M~ (sorted),
-  // I~ (grid order), warp-tile thresholds, stats, exp table
+  const int64_t nwt = (ngrid + kWarpTile - 1) / kWarpTile;
+  const int64_t ngroups = nwt * kPPT;
+  const int nsplit = choose_splits(nwt, nchunks, c->num_sms, 16);
+  const float* wbox = c->d_wtbox.p;
+  const float* gbox = c->d_wtbox.p + 8 * nwt;
+  // scratch: pass-1 sums and error-bound sums, pass-2 corrections (nsplit x n each), I~, E~
+  // (sorted), I~ (grid order), sub-tile thresholds, per-point thresholds, stats, exp table
   const size_t nd = 3 * static_cast<size_t>(nsplit) * ngrid + 3 * static_cast<size_t>(ngrid);
-  const size_t need = sizeof(double) * nd + sizeof(float) * nwt + 64 + sizeof(float2) * (kExpTab + 1) + 256;
+  const size_t need =
+      sizeof(double) * nd + sizeof(float) * (ngroups + ngrid) + 128 + sizeof(float2) * (kExpTab + 1) + 256;
   if (c->d_scratch.reserve(need)) return set_error(c, INCA_E_NOMEM, "mixed scratch");
   double* p1 = reinterpret_cast<double*>(c->d_scratch.p);
   double* pabs = p1 + static_cast<size_t>(nsplit) * ngrid;
   double* p2 = pabs + static_cast<size_t>(nsplit) * ngrid;
   double* Is = p2 + static_cast<size_t>(nsplit) * ngrid;  // I~ in sorted order
-  double* Ms = Is + ngrid;                                 // M~ in sorted order
+  double* Ms = Is + ngrid;                                 // E~ in sorted order
   double* Io = Ms + ngrid;                                 // I~ in grid order (thresholds)
-  float* wlt = reinterpret_cast<float*>(Io + ngrid);
+  float* glt = reinterpret_cast<float*>(Io + ngrid);
+  float* ptau = glt + ngroups;
   unsigned long long* stats =
-      reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(wlt + nwt) + 15) & ~uintptr_t(15));
-  float2* tab = reinterpret_cast<float2*>(stats + 4);
+      reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(ptau + ngrid) + 15) & ~uintptr_t(15));
+  int* errw = reinterpret_cast<int*>(stats + 4);
+  float2* tab = reinterpret_cast<float2*>(stats + 6);
   const std::vector<float2> htab = exp2_table();
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
-  INCA_CUDA(c, cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(stats, 0, 6 * sizeof(unsigned long long), c->stream));
   INCA_CUDA(c, cudaEventRecord(ev[1], c->stream));
-  dim3 grid(static_cast<unsigned>(ctas), static_cast<unsigned>(nsplit));
-  INCA_LAUNCH(c, k_pass1, grid, kThreadsM, 0, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-              c->d_plo.p, c->d_wtbox.p, ngrid, nsplit, p1, pabs, stats);
+  int max_stride = 4;
+  for (const ClassSeg& sg : c->classes) max_stride = std::max(max_stride, sg.stride32);
+  if (max_stride > kMaxStride32) return set_error(c, INCA_E_LIMIT, "inca_eval: record stride above the maximum");
+  const int stage_floats = kChunkMax * max_stride;
+  const size_t dsmem = 128 + 2 * sizeof(float) * stage_floats;
+  dim3 grid(static_cast<unsigned>(nwt), static_cast<unsigned>(nsplit));
+  INCA_LAUNCH(c, k_pass1, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+              c->d_plo.p, wbox, ngrid, nsplit, stage_floats, p1, pabs, stats, errw);
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaEventRecord(ev[2], c->stream));
   INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
@@ -676,9 +958,9 @@ int eval_mixed(inca_ctx* c, double eps) {
     segT.resize(nseg);
     for (int s = 0; s < nseg; ++s) {
       const double O = h[3 * s], M = h[3 * s + 1];
-      const double lo = std::max(std::fabs(O) - 3.0 * kKappaU * M, 0.0);
-      const double x = eps * lo / (3.0 * kKappaU);
-      segT[s] = M > 0.0 ? x * x / M : HUGE_VAL;
+      const double lo = std::max(std::fabs(O) - M, 0.0);
+      const double x = eps * lo;
+      segT[s] = M > 0.0 ? kTauScale * x * x / M : HUGE_VAL;
     }
   } else if (c->grid_kind == GRID_CUBE) {
     mode = 1;
@@ -694,8 +976,8 @@ int eval_mixed(inca_ctx* c, double eps) {
     INCA_CUDA(c, cudaStreamSynchronize(c->stream));
     double Imax;
     std::memcpy(&Imax, &hm, sizeof(double));
-    const double x = eps * Imax / (3.0 * kKappaU);
-    segT = {x * x};
+    const double x = eps * Imax;
+    segT = {kTauScale * x * x};
   } else {
     segT = {0.0};
   }
@@ -704,12 +986,12 @@ int eval_mixed(inca_ctx* c, double eps) {
     return set_error(c, INCA_E_NOMEM, "thresholds");
   }
   INCA_CUDA(c, cudaMemcpyAsync(dT.p, segT.data(), sizeof(double) * segT.size(), cudaMemcpyHostToDevice, c->stream));
-  INCA_LAUNCH(c, k_warp_thresholds, static_cast<unsigned>((nwt + 7) / 8), 256, 0, ngrid, nwt, mode, c->d_perm.p,
-              seg_of, dT.p, c->d_w.p, Is, Ms, eps, wlt);
+  INCA_LAUNCH(c, k_thresholds, static_cast<unsigned>((ngroups + 7) / 8), 256, 0, ngrid, ngroups, mode, c->d_perm.p,
+              seg_of, dT.p, c->d_w.p, Is, Ms, eps, glt, ptau);
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaEventRecord(ev[3], c->stream));
-  INCA_LAUNCH(c, k_pass2, grid, kThreadsM, 0, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-              c->d_plo.p, c->d_wtbox.p, wlt, tab, ngrid, nsplit, p2, stats);
+  INCA_LAUNCH(c, k_pass2, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+              c->d_plo.p, wbox, gbox, glt, ptau, tab, ngrid, nsplit, stage_floats, p2, stats, errw);
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaEventRecord(ev[4], c->stream));
   INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, p2, Is);
@@ -723,16 +1005,20 @@ int eval_mixed(inca_ctx* c, double eps) {
   cudaEventElapsedTime(&t34, ev[3], ev[4]);
   cudaEventElapsedTime(&t05, ev[0], ev[5]);
   for (auto& e : ev) cudaEventDestroy(e);
-  unsigned long long hs[3] = {0, 0, 0};
+  unsigned long long hs[4] = {0, 0, 0, 0};
+  int herr = 0;
   INCA_CUDA(c, cudaMemcpy(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost));
+  INCA_CUDA(c, cudaMemcpy(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return set_error(c, INCA_E_TIMEOUT, "inca_eval: a bounded wait for a staged quartet chunk gave up");
   c->t_total_ms = t05;
-  c->t_kernel_ms = t12;  // the dominant kernel (pass 1)
+  c->t_kernel_ms = t12;  // pass 1
   c->t_pass2_ms = t34;
   c->t_kernel_launches = 1;
   c->t_launches = 9;
   c->pairs_fp32 = static_cast<int64_t>(hs[0]);
   c->pairs_fp64 = static_cast<int64_t>(hs[1]);
   c->pairs_skip = static_cast<int64_t>(hs[2]);
+  c->corrected_points = static_cast<int64_t>(hs[3]) * 32;
   return INCA_OK;
 }
 

@@ -317,7 +317,15 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
     kappa[d] = big > 0.0 ? big : 1.0;
     Bmax = Bmax * kappa[d];
   }
-  const double Aprime = rec.A * Bmax;
+  // a constant polynomial (L_d = 0) normalises to +-1: fold the sign into A' so the
+  // evaluation can skip that dimension (V_d = 1 exactly)
+  double sign = 1.0;
+  for (int d = 0; d < 3; ++d)
+    if (rec.L[d] == 0 && Cu[d][0] < 0.0) {
+      sign = -sign;
+      Cu[d][0] = -Cu[d][0];
+    }
+  const double Aprime = sign * rec.A * Bmax;
   r64[0] = rec.A;
   r64[1] = rec.sqe;
   r64[2] = rec.d[0];

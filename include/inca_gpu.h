@@ -158,10 +158,11 @@ int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
                           int32_t* kernel_launches, int32_t* launches);
 
 /* Work split of the last INCA_MIXED evaluation, in (quartet, 128-point tile) pairs: kept in
- * FP32, corrected in double-float arithmetic (the precise tier), skipped (bound below 2^-120).
- * The FP64 form reports zeros. Pointers may be NULL. */
+ * FP32, examined for corrections (the precise tier), skipped (bound below 2^-120); and the
+ * number of (quartet, point) terms re-evaluated in double-float arithmetic (counted in warps
+ * of 32 points). The FP64 form reports zeros. Pointers may be NULL. */
 int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* precise_pairs,
-                         int64_t* skipped_pairs);
+                         int64_t* skipped_pairs, int64_t* corrected_terms);
 
 /* Device milliseconds of the two passes of the last INCA_MIXED evaluation (estimate pass over
  * all terms; correction pass). The FP64 form reports its single kernel as pass 1. */
