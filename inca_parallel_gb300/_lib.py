@@ -57,6 +57,7 @@ SIGNATURES = {
     "inca_get_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
+    "inca_eval_records_noalloc": (ctypes.c_int, [ctypes.c_int64, VP, VP, VP, VP, VP, ctypes.c_int64, VP, VP, VP]),
 }
 
 _lib = None

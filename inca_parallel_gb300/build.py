@@ -28,6 +28,7 @@ UNITS = {
     "intracule_eval.cu": [],
     "mixed_eval.cu": [],
     "grid_build.cu": ["-fmad=false"],
+    "noalloc_eval.cu": [],
     "host_tables.cpp": [],
 }
 DRIVER_SRC = os.path.join(CSRC, "driver", "inca_main.cpp")

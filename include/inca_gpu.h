@@ -176,6 +176,39 @@ int inca_get_stream(inca_ctx* ctx, void** stream);
  * (library kernels such as CUB sorts are not counted). */
 int inca_kernel_launches(inca_ctx* ctx, int64_t* count);
 
+/* ---------------------------------------------------------------------------------------
+ * Evaluation without allocation. No counterpart in the reference (the Fortran program
+ * allocates its work arrays itself); this entry point exists for callers that must not
+ * allocate device memory while they run: a solver that keeps all its device memory in its
+ * own pool or arena, a long-running service that allocates only at start-up so that it
+ * can never fail for lack of memory later, or a host that records its GPU work for replay.
+ * The context API above cannot serve them, because inca_eval grows its buffers with
+ * cudaMalloc.
+ *
+ * Computes ivec[g] = sum_q A[q] exp(-|r'|^2) Vx(r'_x) Vy(r'_y) Vz(r'_z),
+ * r' = sqe[q] (r_g + d_q), in FP64, for nrec survivor records laid out as inca_get_records
+ * returns them (A[nrec], sqe[nrec], d[nrec][3], L[nrec][3] with 0 <= L <= INCA_MAX_DEGREE,
+ * C[nrec][3][INCA_MAX_DEGREE+1] highest degree first) and npts points r[npts][3].
+ * Every pointer is DEVICE memory owned by the caller, on the current device; the work is
+ * queued on `stream` (a cudaStream_t; NULL is the legacy default stream) and the call
+ * returns without waiting for it. The result equals inca_eval(INCA_FP64) on the same
+ * records and points up to summation order.
+ *
+ * Limits and behaviour:
+ *  - npts <= INCA_NOALLOC_MAX_POINTS; a larger npts returns INCA_E_LIMIT and queues nothing.
+ *    The intermediate sums live in a fixed 16 MiB device array inside the library.
+ *  - The first call on a device sets that device up (it looks up the address of the fixed
+ *    array); make that first call before any stream capture begins.
+ *  - Calls that overlap in time on one device (different streams or host threads) share the
+ *    fixed array and race: order them, e.g. on one stream.
+ *  - Status codes only (there is no context for inca_last_error): INCA_E_ARG for negative
+ *    sizes or null pointers, INCA_E_LIMIT as above, INCA_E_CUDA for a launch failure.
+ */
+#define INCA_NOALLOC_MAX_POINTS (1 << 21)
+int inca_eval_records_noalloc(int64_t nrec, const double* A, const double* sqe,
+                              const double* d, const int32_t* L, const double* C,
+                              int64_t npts, const double* r, double* ivec, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
