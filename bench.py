@@ -40,7 +40,7 @@ FP32_LANES_PER_SM = 128
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
@@ -74,7 +74,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -201,6 +201,7 @@ def gpu_arm(args):
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
+        n0 = ctx.kernel_launches()
         t_wall = time.perf_counter()
         for _ in range(k):
             flush.zero_()
@@ -213,17 +214,17 @@ def gpu_arm(args):
             times.append(e0.elapsed_time(e1))
             kern.append(ctx.phases())
         torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+        launched = ctx.kernel_launches() - n0
         if world > 1:
             torch.distributed.barrier()
-        return times, kern, time.perf_counter() - t_wall, out
+        return times, kern, t_wall, out, launched
 
     # FP64 reference form (plain GPU form), fewer steps (it is ~2 orders slower)
-    t64, k64, _, I64 = timed(INCA_FP64, 0.0, max(2, args.steps // 3), 1)
+    t64, k64, _, I64, _ = timed(INCA_FP64, 0.0, max(2, args.steps // 3), 1)
     # mixed form: the headline
-    launches0 = ctx.kernel_launches()
     with ClockSampler(local) as clk:
-        tm, km, wall, Imix = timed(INCA_MIXED, TOL_SCAN, args.steps, args.warmup)
-    launches = (ctx.kernel_launches() - launches0) // (args.steps + args.warmup)
+        tm, km, wall, Imix, launches = timed(INCA_MIXED, TOL_SCAN, args.steps, args.warmup)
     stats = ctx.stats()
     ms = statistics.mean(tm)
     ms64 = statistics.mean(t64)

@@ -88,6 +88,11 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_plo.release();
   c->d_perm.release();
   c->d_wtbox.release();
+  c->d_phi_s.release();
+  c->d_plo_s.release();
+  c->d_perm_s.release();
+  c->d_wtbox_s.release();
+  c->d_scratch_s.release();
   cudaStreamDestroy(c->stream);
   delete c;
   return INCA_OK;

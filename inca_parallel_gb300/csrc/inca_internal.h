@@ -128,6 +128,13 @@ struct inca_ctx {
   inca::DevBuf<float4> d_phi, d_plo;  // FP32 hi / lo parts of the sorted points
   inca::DevBuf<int64_t> d_perm;       // sorted position -> grid index
   inca::DevBuf<float> d_wtbox;        // per 128-point warp tile: lo[3], hi[3], 2 pad
+  // the same for a strided sample of the grid (threshold estimates of the one-pass form)
+  int64_t sample_version = -1;
+  int64_t nsample = 0;
+  inca::DevBuf<float4> d_phi_s, d_plo_s;
+  inca::DevBuf<int64_t> d_perm_s;
+  inca::DevBuf<float> d_wtbox_s;
+  inca::DevBuf<unsigned char> d_scratch_s;
 
   // scratch
   inca::DevBuf<double> d_partial;

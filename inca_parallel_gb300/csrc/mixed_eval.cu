@@ -35,6 +35,7 @@
 //   pass 1).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -56,6 +57,16 @@ constexpr int kChunkMax = 32;
 // round-to-nearest errors bounded in total by e_t, so its variance is <= e_t^2 / 3, and
 // 3 sigma <= eps |O| gives tau <= 3 (eps |O| / 3)^2 / E_O.
 constexpr double kTauScale = 1.0 / 3.0;
+constexpr double kTestScale = 1.0 / 1.01;  // correct when e > tau / 1.01
+// One-pass form (grids of at least kFuseMinPoints points): thresholds are estimated from every
+// kSampleStride-th grid point, scaled down by kEstSafety (and, for the max-norm of cubes, with
+// the largest sampled error sum times kCubeMargin standing in for each point's); where the
+// exact thresholds after the pass are lower than the estimates, a correction pass covers the
+// difference.
+constexpr int64_t kFuseMinPoints = 16384;
+constexpr int64_t kSampleStride = 16;
+constexpr double kEstSafety = 0.5;
+constexpr double kCubeMargin = 2.0;
 constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kExpTab = 256;             // 2^(j/256), j = -128..128
 constexpr int kFold = 8;                 // chunks between FP64 folds
@@ -476,19 +487,39 @@ __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chun
 }
 
 // ---------------------------------------------------------------- pass 1
+// kFuse = false: estimate pass (every term in FP32, exact accumulation, error-bound sums).
+// kFuse = true: one-pass form. Thresholds tau_g estimated beforehand (pt_tau) select the terms
+//   to correct while they are evaluated: such a term's FP32 value is left out of the sum, the
+//   lanes note (quartet, point) in a mask, and after each chunk the warp evaluates the noted
+//   terms in double-float, each lane working down its own list (the chunk is class-uniform,
+//   so the lanes run the same instruction sequence on different quartets).
+template <bool kFuse>
 __global__ void __launch_bounds__(32, 16)
 k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
-        const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part,
+        const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats,
+        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, double* __restrict__ part,
         double* __restrict__ part_abs, unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
+  __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
   const int lane = threadIdx.x;
   const int64_t wtile = blockIdx.x;
   const int64_t base = wtile * kWarpTile;
   stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
   float rh[3][kPPT], rl[3][kPPT];
   load_points(phi, plo, base, lane, ngrid, rh, rl);
+  float tau[kPPT];
+  f2 corr[kPPT];
+  if (kFuse) {
+    for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) {
+      const int64_t i = base + lane + 32 * p;
+      tau[p] = i < ngrid ? pt_tau[i] : HUGE_VALF;
+      corr[p] = {0.0f, 0.0f};
+    }
+  }
   float box[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) box[k] = wtbox[wtile * 8 + k];
@@ -499,7 +530,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     acc[p] = 0.0;
     sh[p] = sl[p] = sa[p] = 0.0f;
   }
-  unsigned long long nskip = 0;
+  __syncwarp();
+  unsigned long long nskip = 0, nlive = 0, ncorr = 0, nround = 0;
   int nfold = 0, k = 0;
   for (int ch = blockIdx.y; ch < nchunks; ch += nsplit, ++k) {
     if (!stage_next(S, chunks, segs, rec32, k, ch + nsplit, nchunks)) {
@@ -512,7 +544,13 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
     const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
     uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > kSkipLog2);
-    if (lane == 0) nskip += w.count - __popc(m);
+    if (lane == 0) {
+      nskip += w.count - __popc(m);
+      nlive += __popc(m);
+    }
+    uint32_t nm[kPPT];
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) nm[p] = 0u;
     while (m) {
       const int q = __ffs(m) - 1;
       m &= m - 1;
@@ -520,10 +558,31 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
       terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
+        if (kFuse && e[p] > tau[p]) {
+          nm[p] |= 1u << q;
+          t[p] = 0.0f;
+        }
         const f2 s = two_sum(sh[p], t[p]);
         sh[p] = s.hi;
         sl[p] = __fadd_rn(sl[p], s.lo);
         sa[p] = __fadd_rn(sa[p], e[p]);
+      }
+    }
+    if (kFuse) {
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) {
+        uint32_t mm = nm[p];
+        while (__any_sync(0xffffffffu, mm != 0u)) {
+          ++nround;
+          if (mm) {
+            const int q = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p],
+                                   rl[1][p], rl[2][p], tab);
+            corr[p] = df_add(corr[p], tdf);
+            ++ncorr;
+          }
+        }
       }
     }
     // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
@@ -536,6 +595,10 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
       if (fold) {
         acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
         sh[p] = sl[p] = 0.0f;
+        if (kFuse) {
+          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+          corr[p] = {0.0f, 0.0f};
+        }
       }
     }
     if (fold) nfold = 0;
@@ -544,13 +607,24 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
 #pragma unroll
   for (int p = 0; p < kPPT; ++p) {
     acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
+    if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
     const int64_t i = base + lane + 32 * p;
     if (i < ngrid) {
       part[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc[p];
       part_abs[static_cast<int64_t>(blockIdx.y) * ngrid + i] = static_cast<double>(sa[p]);
     }
   }
-  if (lane == 0) atomicAdd(&stats[2], nskip);
+  if (kFuse) {
+    for (int o = 16; o > 0; o >>= 1) ncorr += __shfl_xor_sync(0xffffffffu, ncorr, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&stats[2], nskip);
+    if (kFuse) {
+      atomicAdd(&stats[0], nlive);
+      atomicAdd(&stats[1], nround);
+      atomicAdd(&stats[3], ncorr);
+    }
+  }
 }
 
 // ---------------------------------------------------------------- pass 2 (corrections)
@@ -558,8 +632,9 @@ __global__ void __launch_bounds__(32, 16)
 k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
         const float* __restrict__ wtbox, const float* __restrict__ gbox, const float* __restrict__ g_lt,
-        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, int64_t ngrid, int nsplit,
-        int stage_floats, double* __restrict__ part, unsigned long long* __restrict__ stats, int* __restrict__ err) {
+        const float* __restrict__ pt_tau, const float* __restrict__ pt_tau_est, const float2* __restrict__ exp_tab,
+        int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part, unsigned long long* __restrict__ stats,
+        int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kExpTab + 1];
@@ -568,12 +643,13 @@ k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
   const int64_t base = wtile * kWarpTile;
   stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
   for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
-  float rh[3][kPPT], rl[3][kPPT], tau[kPPT];
+  float rh[3][kPPT], rl[3][kPPT], tau[kPPT], tau_est[kPPT];
   load_points(phi, plo, base, lane, ngrid, rh, rl);
 #pragma unroll
   for (int p = 0; p < kPPT; ++p) {
     const int64_t i = base + lane + 32 * p;
     tau[p] = i < ngrid ? pt_tau[i] : HUGE_VALF;
+    tau_est[p] = (pt_tau_est && i < ngrid) ? pt_tau_est[i] : HUGE_VALF;
   }
   float wbox[6];
 #pragma unroll
@@ -625,12 +701,14 @@ k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
         const float* R = st + q * sg.stride32;
         float t32[1], e32[1];
         term32_one(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], t32, e32);
-        const bool need = e32[0] * 1.01f > tau[p];
+        // with pt_tau_est: the one-pass kernel already corrected the live terms above tau_est
+        const bool live_q = (live >> q) & 1u;
+        const bool need = e32[0] > tau[p] && !(live_q && e32[0] > tau_est[p]);
         if (__any_sync(0xffffffffu, need)) {
           if (lane == 0) ++npts;
           if (need) {
             f2 tdf = term_df(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], tab);
-            if ((live >> q) & 1u) tdf = df_add(tdf, f2{-t32[0], 0.0f});
+            if (live_q) tdf = df_add(tdf, f2{-t32[0], 0.0f});
             corr[p] = df_add(corr[p], tdf);
           }
         }
@@ -660,19 +738,34 @@ k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
 }
 
 // ---------------------------------------------------------------- grid preparation
-__global__ void k_morton(int64_t n, const double* __restrict__ px, const double* __restrict__ py,
+// Morton keys of the points g = j * stride, j < n (stride 1: the whole grid).
+__global__ void k_morton(int64_t n, int64_t stride, const double* __restrict__ px, const double* __restrict__ py,
                          const double* __restrict__ pz, double lo0, double lo1, double lo2, double inv,
                          uint64_t* key, int64_t* idx) {
-  const int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (g >= n) return;
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (j >= n) return;
+  const int64_t g = j * stride;
   const double c[3] = {(px[g] - lo0) * inv, (py[g] - lo1) * inv, (pz[g] - lo2) * inv};
   uint64_t k = 0;
   uint32_t q[3];
   for (int d = 0; d < 3; ++d) q[d] = static_cast<uint32_t>(fmin(fmax(c[d], 0.0), 2097151.0));
   for (int b = 20; b >= 0; --b)
     for (int d = 0; d < 3; ++d) k = (k << 1) | ((q[d] >> b) & 1u);
-  key[g] = k;
-  idx[g] = g;
+  key[j] = k;
+  idx[j] = g;
+}
+
+// Each coordinate x is stored as hi + lo (FP32 pair). The split is offset from the nearest
+// float by a pseudo-random number of ulps (|k| <= 32, from a hash of the grid index and the
+// axis): symmetry-equivalent points of a symmetric molecule then round differently in FP32, so
+// the rounding errors of their terms are not copies of one another (the correction thresholds
+// assume independent errors). The pair still represents x to ~2^-42 relative.
+__device__ __forceinline__ int split_offset(int64_t g, int d) {
+  uint64_t z = static_cast<uint64_t>(g) * 3u + static_cast<uint64_t>(d) + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return static_cast<int>(z % 65u) - 32;
 }
 
 __global__ void k_gather_points(int64_t n, const int64_t* __restrict__ perm, const double* __restrict__ px,
@@ -685,6 +778,10 @@ __global__ void k_gather_points(int64_t n, const int64_t* __restrict__ perm, con
   float h[3], l[3];
   for (int d = 0; d < 3; ++d) {
     h[d] = static_cast<float>(x[d]);
+    if (fabsf(h[d]) >= 1.0e-30f) {  // normal and far from zero: step the magnitude by k ulps
+      const int bits = __float_as_int(h[d]);
+      h[d] = __int_as_float((bits & 0x80000000) | ((bits & 0x7FFFFFFF) + split_offset(g, d)));
+    }
     l[d] = static_cast<float>(x[d] - static_cast<double>(h[d]));
   }
   phi[i] = make_float4(h[0], h[1], h[2], 0.0f);
@@ -729,34 +826,90 @@ __global__ void k_boxes(int64_t n, int64_t nwt, const float4* __restrict__ phi, 
     }
 }
 
-// Per-point thresholds tau_g (sorted order) and their minimum per 32-point sub-tile (log2).
-// mode 0: tau = T_o / w_g; mode 1 (max-norm): tau = T_o / E_g; mode 2 (per point).
+// Per-point test thresholds (sorted order) and their minimum per 32-point sub-tile (log2).
+// A term is corrected when its error bound e exceeds tau_g / 1.01 (the stored value).
+// mode 0: tau = T_seg / w_g; mode 1 (max-norm): tau = T / E_g; mode 2: per point;
+// mode 3: tau = T (uniform).
 __global__ void k_thresholds(int64_t n, int64_t ngroups, int mode, const int64_t* __restrict__ perm,
                              const int* __restrict__ seg_of, const double* __restrict__ segT,
                              const double* __restrict__ w, const double* __restrict__ I,
-                             const double* __restrict__ M, double eps, float* g_lt, float* pt_tau) {
+                             const double* __restrict__ M, double eps, double tscale, float* g_lt, float* pt_tau) {
   const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (grp >= ngroups) return;
   const int lane = threadIdx.x & 31;
   // group grp = tile grp / kPPT, sub-tile grp % kPPT: points tile*128 + lane + 32*sub
   const int64_t i = (grp / kPPT) * kWarpTile + lane + 32 * (grp % kPPT);
-  double tau = HUGE_VAL;
+  float ts = HUGE_VALF;
   if (i < n) {
     const int64_t g = perm[i];
+    double tau = HUGE_VAL;
     if (mode == 0) {
       tau = w[g] > 0.0 ? segT[seg_of ? seg_of[g] : 0] / w[g] : HUGE_VAL;
     } else if (mode == 1) {
       tau = M[i] > 0.0 ? segT[0] / M[i] : HUGE_VAL;
-    } else {
+    } else if (mode == 2) {
       const double lo = fmax(fabs(I[i]) - M[i], 0.0);
       const double x = eps * lo;
-      tau = M[i] > 0.0 ? kTauScale * x * x / M[i] : HUGE_VAL;
+      tau = M[i] > 0.0 ? tscale * x * x / M[i] : HUGE_VAL;
+    } else {
+      tau = segT[0];
     }
-    pt_tau[i] = tau >= 3.0e38 ? HUGE_VALF : static_cast<float>(tau);
+    tau *= kTestScale;
+    ts = tau >= 3.0e38 ? HUGE_VALF : static_cast<float>(tau);
+    pt_tau[i] = ts;
   }
-  double tmin = tau;
-  for (int o = 16; o > 0; o >>= 1) tmin = fmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-  if (lane == 0) g_lt[grp] = tmin >= HUGE_VAL ? HUGE_VALF : (tmin > 0.0 ? static_cast<float>(log2(tmin)) : -HUGE_VALF);
+  if (!g_lt) return;
+  float tmin = ts;
+  for (int o = 16; o > 0; o >>= 1) tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+  if (lane == 0) g_lt[grp] = tmin >= HUGE_VALF ? HUGE_VALF : (tmin > 0.0f ? log2f(tmin) : -HUGE_VALF);
+}
+
+// Sub-tiles where the exact threshold fell below the estimate used by the one-pass kernel:
+// g_lt = log2 of the smallest exact threshold among those points (else +inf); counts them.
+__global__ void k_band(int64_t n, int64_t ngroups, const float* __restrict__ pt_tau,
+                       const float* __restrict__ pt_tau_est, float* g_lt, unsigned long long* nband) {
+  const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
+  if (grp >= ngroups) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (grp / kPPT) * kWarpTile + lane + 32 * (grp % kPPT);
+  float t = HUGE_VALF;
+  if (i < n && pt_tau[i] < pt_tau_est[i]) t = pt_tau[i];
+  for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
+  if (lane == 0) {
+    g_lt[grp] = t >= HUGE_VALF ? HUGE_VALF : (t > 0.0f ? log2f(t) : -HUGE_VALF);
+    if (t < HUGE_VALF) atomicAdd(nband, 1ull);
+  }
+}
+
+// Sampled estimates, scattered to grid order: I and E at the sampled points, their weights
+// (zero elsewhere; the targets are cleared first).
+__global__ void k_scatter_sample(int64_t n, const int64_t* __restrict__ perm, const double* __restrict__ I,
+                                 const double* __restrict__ M, const double* __restrict__ w, double* Io,
+                                 double* Mo, double* wo) {
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (j >= n) return;
+  const int64_t g = perm[j];
+  Io[g] = I[j];
+  Mo[g] = M[j];
+  if (w) wo[g] = w[g];
+}
+
+__global__ void k_absmax2(int64_t n, const double* __restrict__ I, const double* __restrict__ M,
+                          unsigned long long* out) {
+  double a = 0.0, b = 0.0;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < n;
+       g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    a = fmax(a, fabs(I[g]));
+    b = fmax(b, fabs(M[g]));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], static_cast<unsigned long long>(__double_as_longlong(a)));
+    atomicMax(&out[1], static_cast<unsigned long long>(__double_as_longlong(b)));
+  }
 }
 
 // Sum the split partials of the passes (sorted order) in a fixed order.
@@ -802,25 +955,48 @@ __global__ void k_seg_sums(int nseg, const int64_t* __restrict__ off, const doub
     for (int j = 0; j < 3; ++j) out[3 * seg + j] = s[j][0];
 }
 
-__global__ void k_absmax(int64_t n, const double* __restrict__ I, unsigned long long* out) {
-  double m = 0.0;
-  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < n;
-       g += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    m = fmax(m, fabs(I[g]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(m)));
-}
-
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
-// Morton-sorted FP32 copy of the grid, the permutation and the tile / sub-tile boxes.
-int prepare_sorted_grid(inca_ctx* c) {
-  if (c->mix_version == c->grid_version) return INCA_OK;
-  const int64_t n = c->ngrid;
+// Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
+// permutation (sorted position -> grid index) and the tile / sub-tile boxes.
+int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, DevBuf<float4>& phi,
+                DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, int64_t* n_out) {
+  const int64_t n = (c->ngrid + stride - 1) / stride;
   const int64_t nwt = (n + kWarpTile - 1) / kWarpTile;
-  if (c->d_phi.reserve(n) || c->d_plo.reserve(n) || c->d_perm.reserve(n) ||
-      c->d_wtbox.reserve(8 * nwt + 8 * nwt * kPPT))
+  if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
+  DevBuf<uint64_t> k1, k2;
+  DevBuf<int64_t> i1;
+  DevBuf<unsigned char> tmp;
+  auto rel = [&]() { k1.release(); k2.release(); i1.release(); tmp.release(); };
+  if (k1.reserve(n) || k2.reserve(n) || i1.reserve(n)) {
+    rel();
+    return set_error(c, INCA_E_NOMEM, "morton sort");
+  }
+  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p, lo[0], lo[1], lo[2], inv,
+              k1.p, i1.p);
+  size_t tb = 0;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
+  if (!e) e = tmp.reserve(tb);
+  if (!e) e = cub::DeviceRadixSort::SortPairs(tmp.p, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
+  if (!e) {
+    INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, phi.p, plo.p);
+    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, n, nwt, phi.p, plo.p, boxes.p,
+                boxes.p + 8 * nwt);
+    e = cudaStreamSynchronize(c->stream);
+  }
+  rel();
+  if (e) return cuda_error(c, e, "sorted grid");
+  *n_out = n;
+  return INCA_OK;
+}
+
+// The sorted grid (and, for the one-pass form, the sorted sample), rebuilt when the grid changes.
+int prepare_sorted_grid(inca_ctx* c, bool sample) {
+  const bool main_ok = c->mix_version == c->grid_version;
+  const bool sample_ok = !sample || c->sample_version == c->grid_version;
+  if (main_ok && sample_ok) return INCA_OK;
+  const int64_t n = c->ngrid;
   // bounding box of the grid (one host copy of the coordinates; cheap next to evaluation)
   std::vector<double> hx(n), hy(n), hz(n);
   INCA_CUDA(c, cudaMemcpy(hx.data(), c->d_px.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
@@ -834,31 +1010,41 @@ int prepare_sorted_grid(inca_ctx* c) {
   }
   const double ext = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-12));
   const double inv = 2097151.0 / ext;
-  DevBuf<uint64_t> k1, k2;
-  DevBuf<int64_t> i1;
-  DevBuf<unsigned char> tmp;
-  auto rel = [&]() { k1.release(); k2.release(); i1.release(); tmp.release(); };
-  if (k1.reserve(n) || k2.reserve(n) || i1.reserve(n)) {
-    rel();
-    return set_error(c, INCA_E_NOMEM, "morton sort");
+  int64_t nn = 0;
+  if (!main_ok) {
+    const int st = sort_points(c, 1, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, &nn);
+    if (st) return st;
+    c->mix_version = c->grid_version;
   }
-  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, c->d_px.p, c->d_py.p, c->d_pz.p, lo[0], lo[1], lo[2], inv, k1.p, i1.p);
-  size_t tb = 0;
-  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb, k1.p, k2.p, i1.p, c->d_perm.p, n, 0, 63, c->stream);
-  if (!e) e = tmp.reserve(tb);
-  if (!e) e = cub::DeviceRadixSort::SortPairs(tmp.p, tb, k1.p, k2.p, i1.p, c->d_perm.p, n, 0, 63, c->stream);
-  if (!e) {
-    INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, c->d_perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_phi.p,
-                c->d_plo.p);
-    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, n, nwt, c->d_phi.p, c->d_plo.p,
-                c->d_wtbox.p, c->d_wtbox.p + 8 * nwt);
-    e = cudaStreamSynchronize(c->stream);
+  if (!sample_ok) {
+    const int st = sort_points(c, kSampleStride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
+                               &c->nsample);
+    if (st) return st;
+    c->sample_version = c->grid_version;
   }
-  rel();
-  if (e) return cuda_error(c, e, "sorted grid");
-  c->mix_version = c->grid_version;
   return INCA_OK;
 }
+
+// Bump allocator over a scratch buffer: a dry run (base == nullptr) measures the size.
+struct Carve {
+  unsigned char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+struct Events {
+  cudaEvent_t e[6] = {};
+  ~Events() {
+    for (auto& x : e)
+      if (x) cudaEventDestroy(x);
+  }
+};
 
 // 2^(j/256), j = -128..128, as float pairs (host, double precision).
 std::vector<float2> exp2_table() {
@@ -881,144 +1067,259 @@ int eval_mixed(inca_ctx* c, double eps) {
     INCA_CUDA(c, cudaStreamSynchronize(c->stream));
     return INCA_OK;
   }
-  cudaEvent_t ev[6];
-  for (auto& e : ev) INCA_CUDA(c, cudaEventCreate(&e));
-  INCA_CUDA(c, cudaEventRecord(ev[0], c->stream));
-  int st = prepare_sorted_grid(c);
+  const int64_t launches0 = c->launches;
+  const bool fused =
+      (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN || c->grid_kind == GRID_CUBE) && ngrid >= kFuseMinPoints;
+  Events ev;
+  for (auto& e : ev.e) INCA_CUDA(c, cudaEventCreate(&e));
+  INCA_CUDA(c, cudaEventRecord(ev.e[0], c->stream));
+  int st = prepare_sorted_grid(c, fused);
   if (st) return st;
   const int64_t nwt = (ngrid + kWarpTile - 1) / kWarpTile;
   const int64_t ngroups = nwt * kPPT;
   const int nsplit = choose_splits(nwt, nchunks, c->num_sms, 16);
   const float* wbox = c->d_wtbox.p;
   const float* gbox = c->d_wtbox.p + 8 * nwt;
-  // scratch: pass-1 sums and error-bound sums, pass-2 corrections (nsplit x n each), I~, E~
-  // (sorted), I~ (grid order), sub-tile thresholds, per-point thresholds, stats, exp table
-  const size_t nd = 3 * static_cast<size_t>(nsplit) * ngrid + 3 * static_cast<size_t>(ngrid);
-  const size_t need =
-      sizeof(double) * nd + sizeof(float) * (ngroups + ngrid) + 128 + sizeof(float2) * (kExpTab + 1) + 256;
-  if (c->d_scratch.reserve(need)) return set_error(c, INCA_E_NOMEM, "mixed scratch");
-  double* p1 = reinterpret_cast<double*>(c->d_scratch.p);
-  double* pabs = p1 + static_cast<size_t>(nsplit) * ngrid;
-  double* p2 = pabs + static_cast<size_t>(nsplit) * ngrid;
-  double* Is = p2 + static_cast<size_t>(nsplit) * ngrid;  // I~ in sorted order
-  double* Ms = Is + ngrid;                                 // E~ in sorted order
-  double* Io = Ms + ngrid;                                 // I~ in grid order (thresholds)
-  float* glt = reinterpret_cast<float*>(Io + ngrid);
-  float* ptau = glt + ngroups;
-  unsigned long long* stats =
-      reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(ptau + ngrid) + 15) & ~uintptr_t(15));
-  int* errw = reinterpret_cast<int*>(stats + 4);
-  float2* tab = reinterpret_cast<float2*>(stats + 6);
+
+  // outputs and their segments: radial grid (one integral), scan grid (one I(s) per shell),
+  // cube (max-norm), explicit points (each point)
+  int mode = 2;
+  std::vector<int64_t> off;
+  const int* seg_of = nullptr;
+  if (c->grid_kind == GRID_RADIAL) {
+    mode = 0;
+    off = {0, ngrid};
+  } else if (c->grid_kind == GRID_SCAN) {
+    mode = 0;
+    off.assign(c->nradi + 1, 0);
+    for (int s = 0; s < c->nradi; ++s) off[s + 1] = off[s] + c->h_smn[s];
+    seg_of = c->d_cmap.p;  // shell of each scan point
+  } else if (c->grid_kind == GRID_CUBE) {
+    mode = 1;
+  }
+  const int nseg = off.empty() ? 1 : static_cast<int>(off.size()) - 1;
+
+  // scratch: pass sums and error-bound sums (nsplit x n), I~ / E~ sorted and grid order,
+  // thresholds, statistics, the exp table, segment sums
+  double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT;
+  float *glt, *ptau, *ptau_est;
+  unsigned long long *stats, *dmax;
+  int* errw;
+  int64_t* doff;
+  float2* tab;
+  auto layout = [&](Carve& cv) {
+    p1 = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
+    pabs = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
+    p2 = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
+    Is = cv.take<double>(ngrid);
+    Ms = cv.take<double>(ngrid);
+    Io = cv.take<double>(ngrid);
+    Mo = cv.take<double>(ngrid);
+    glt = cv.take<float>(ngroups);
+    ptau = cv.take<float>(ngrid);
+    ptau_est = cv.take<float>(fused ? ngrid : 1);
+    stats = cv.take<unsigned long long>(16);
+    dmax = cv.take<unsigned long long>(2);
+    errw = cv.take<int>(4);
+    tab = cv.take<float2>(kExpTab + 1);
+    dout = cv.take<double>(6 * nseg);
+    dT = cv.take<double>(nseg);
+    doff = cv.take<int64_t>(nseg + 1);
+  };
+  Carve dry{nullptr};
+  layout(dry);
+  if (c->d_scratch.reserve(dry.off + 256)) return set_error(c, INCA_E_NOMEM, "mixed scratch");
+  Carve cv{c->d_scratch.p};
+  layout(cv);
+  // INCA_TAU_SCALE overrides the variance factor of the thresholds (tuning and test knob)
+  double tau_scale = kTauScale;
+  if (const char* env = std::getenv("INCA_TAU_SCALE")) {
+    char* end = nullptr;
+    const double v = std::strtod(env, &end);
+    if (end != env && v > 0.0 && std::isfinite(v)) tau_scale = v;
+  }
   const std::vector<float2> htab = exp2_table();
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
-  INCA_CUDA(c, cudaMemsetAsync(stats, 0, 6 * sizeof(unsigned long long), c->stream));
-  INCA_CUDA(c, cudaEventRecord(ev[1], c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(errw, 0, 4 * sizeof(int), c->stream));
+  if (!off.empty())
+    INCA_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
   int max_stride = 4;
   for (const ClassSeg& sg : c->classes) max_stride = std::max(max_stride, sg.stride32);
   if (max_stride > kMaxStride32) return set_error(c, INCA_E_LIMIT, "inca_eval: record stride above the maximum");
   const int stage_floats = kChunkMax * max_stride;
   const size_t dsmem = 128 + 2 * sizeof(float) * stage_floats;
+  const unsigned gblk = static_cast<unsigned>((ngroups + 7) / 8);
+  std::vector<double> hseg(6 * nseg), segT(nseg);
+
+  // segment sums of w I~, w E~, w (first three) and, with a second weight array, w2 (sixth)
+  auto seg_sums = [&](const double* w, const double* I, const double* M, const double* w2) -> int {
+    INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, w, I, M, dout);
+    if (w2) INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, w2, I, M, dout + 3 * nseg);
+    INCA_CUDA(c, cudaMemcpyAsync(hseg.data(), dout, sizeof(double) * (w2 ? 6 : 3) * nseg, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return INCA_OK;
+  };
+  auto absmax = [&](const double* I, const double* M, int64_t n, double* imax, double* emax) -> int {
+    INCA_CUDA(c, cudaMemsetAsync(dmax, 0, 2 * sizeof(unsigned long long), c->stream));
+    const unsigned nb = static_cast<unsigned>(std::min<int64_t>(nblk(n), 4096));
+    INCA_LAUNCH(c, k_absmax2, nb, 256, 0, n, I, M, dmax);
+    unsigned long long hm[2] = {0, 0};
+    INCA_CUDA(c, cudaMemcpyAsync(hm, dmax, sizeof(hm), cudaMemcpyDeviceToHost, c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(imax, &hm[0], sizeof(double));
+    std::memcpy(emax, &hm[1], sizeof(double));
+    return INCA_OK;
+  };
+  auto tau_of = [&](double O, double M) {
+    const double lo = std::max(std::fabs(O) - M, 0.0);
+    const double x = eps * lo;
+    return M > 0.0 ? tau_scale * x * x / M : HUGE_VAL;
+  };
+
+  // ---- threshold estimates from the grid sample (one-pass form)
+  if (fused) {
+    // INCA_EST_SAFETY overrides the factor applied to the estimated thresholds (a test and
+    // tuning knob: larger values trade correction-pass work for one-pass work)
+    double safety = kEstSafety;
+    if (const char* env = std::getenv("INCA_EST_SAFETY")) {
+      char* end = nullptr;
+      const double v = std::strtod(env, &end);
+      if (end != env && v >= 0.0 && std::isfinite(v)) safety = v;
+    }
+    const int64_t ns = c->nsample;
+    const int64_t nwt_s = (ns + kWarpTile - 1) / kWarpTile;
+    const int nsplit_s = choose_splits(nwt_s, nchunks, c->num_sms, 16);
+    double *q1, *qabs, *Iss, *Mss, *Ios, *Mos, *ws;
+    auto layout_s = [&](Carve& cs) {
+      q1 = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);
+      qabs = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);
+      Iss = cs.take<double>(ns);
+      Mss = cs.take<double>(ns);
+      Ios = cs.take<double>(ngrid);
+      Mos = cs.take<double>(ngrid);
+      ws = cs.take<double>(ngrid);
+    };
+    Carve dry_s{nullptr};
+    layout_s(dry_s);
+    if (c->d_scratch_s.reserve(dry_s.off + 256)) return set_error(c, INCA_E_NOMEM, "sample scratch");
+    Carve cs{c->d_scratch_s.p};
+    layout_s(cs);
+    dim3 grid_s(static_cast<unsigned>(nwt_s), static_cast<unsigned>(nsplit_s));
+    INCA_LAUNCH(c, k_pass1<false>, grid_s, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
+                c->d_phi_s.p, c->d_plo_s.p, c->d_wtbox_s.p, ns, nsplit_s, stage_floats, nullptr, nullptr, q1, qabs,
+                stats + 8, errw);
+    INCA_CUDA(c, cudaGetLastError());
+    INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, q1, nullptr, Iss);
+    INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, qabs, nullptr, Mss);
+    int emode = 0;
+    if (mode == 0) {
+      INCA_CUDA(c, cudaMemsetAsync(Ios, 0, sizeof(double) * ngrid, c->stream));
+      INCA_CUDA(c, cudaMemsetAsync(Mos, 0, sizeof(double) * ngrid, c->stream));
+      INCA_CUDA(c, cudaMemsetAsync(ws, 0, sizeof(double) * ngrid, c->stream));
+      INCA_LAUNCH(c, k_scatter_sample, nblk(ns), 256, 0, ns, c->d_perm_s.p, Iss, Mss, c->d_w.p, Ios, Mos, ws);
+      if ((st = seg_sums(ws, Ios, Mos, c->d_w.p))) return st;
+      for (int s = 0; s < nseg; ++s) {
+        const double wsam = hseg[3 * s + 2], wtot = hseg[3 * nseg + 3 * s + 2];
+        const double f = wsam > 0.0 ? wtot / wsam : 0.0;
+        const double t = tau_of(hseg[3 * s] * f, hseg[3 * s + 1] * f);
+        segT[s] = (wsam > 0.0 && hseg[3 * s + 1] > 0.0) ? safety * t : 0.0;
+      }
+    } else {
+      emode = 3;
+      double imax = 0.0, emax = 0.0;
+      if ((st = absmax(Iss, Mss, ns, &imax, &emax))) return st;
+      const double x = eps * imax;
+      segT[0] = emax > 0.0 ? safety * tau_scale * x * x / (kCubeMargin * emax) : 0.0;
+    }
+    INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
+    INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
+                nullptr, eps, tau_scale, nullptr, ptau_est);
+    INCA_CUDA(c, cudaGetLastError());
+  }
+
+  // ---- the pass over all terms (one-pass form: with corrections above the estimates)
+  INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
   dim3 grid(static_cast<unsigned>(nwt), static_cast<unsigned>(nsplit));
-  INCA_LAUNCH(c, k_pass1, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-              c->d_plo.p, wbox, ngrid, nsplit, stage_floats, p1, pabs, stats, errw);
+  if (fused)
+    INCA_LAUNCH(c, k_pass1<true>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+                c->d_plo.p, wbox, ngrid, nsplit, stage_floats, ptau_est, tab, p1, pabs, stats, errw);
+  else
+    INCA_LAUNCH(c, k_pass1<false>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
+                c->d_phi.p, c->d_plo.p, wbox, ngrid, nsplit, stage_floats, nullptr, nullptr, p1, pabs, stats, errw);
   INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev[2], c->stream));
+  INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
   INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
   INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, pabs, nullptr, Ms);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
-  // per-output scales
-  int mode = 2;
-  std::vector<double> segT;
-  const int* seg_of = nullptr;
-  DevBuf<double> dT, dout, Mo;
-  DevBuf<int64_t> doff;
-  DevBuf<unsigned long long> dmax;
-  auto rel = [&]() { dT.release(); dout.release(); doff.release(); dmax.release(); Mo.release(); };
-  if (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN) {
-    mode = 0;
-    std::vector<int64_t> off;
-    if (c->grid_kind == GRID_RADIAL) {
-      off = {0, ngrid};
-    } else {
-      off.assign(c->nradi + 1, 0);
-      for (int s = 0; s < c->nradi; ++s) off[s + 1] = off[s] + c->h_smn[s];
-      seg_of = c->d_cmap.p;  // shell of each scan point
-    }
-    const int nseg = static_cast<int>(off.size()) - 1;
-    if (doff.reserve(nseg + 1) || dout.reserve(3 * nseg) || Mo.reserve(ngrid)) {
-      rel();
-      return set_error(c, INCA_E_NOMEM, "thresholds");
-    }
-    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Ms, Mo.p);
-    INCA_CUDA(c, cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
-    INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff.p, c->d_w.p, Io, Mo.p, dout.p);
-    std::vector<double> h(3 * nseg);
-    INCA_CUDA(c, cudaMemcpyAsync(h.data(), dout.p, sizeof(double) * 3 * nseg, cudaMemcpyDeviceToHost, c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    segT.resize(nseg);
-    for (int s = 0; s < nseg; ++s) {
-      const double O = h[3 * s], M = h[3 * s + 1];
-      const double lo = std::max(std::fabs(O) - M, 0.0);
-      const double x = eps * lo;
-      segT[s] = M > 0.0 ? kTauScale * x * x / M : HUGE_VAL;
-    }
-  } else if (c->grid_kind == GRID_CUBE) {
-    mode = 1;
-    if (dmax.reserve(1)) {
-      rel();
-      return set_error(c, INCA_E_NOMEM, "thresholds");
-    }
-    INCA_CUDA(c, cudaMemsetAsync(dmax.p, 0, sizeof(unsigned long long), c->stream));
-    const unsigned nb = static_cast<unsigned>(std::min<int64_t>(nblk(ngrid), 4096));
-    INCA_LAUNCH(c, k_absmax, nb, 256, 0, ngrid, Is, dmax.p);
-    unsigned long long hm = 0;
-    INCA_CUDA(c, cudaMemcpyAsync(&hm, dmax.p, sizeof(hm), cudaMemcpyDeviceToHost, c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    double Imax;
-    std::memcpy(&Imax, &hm, sizeof(double));
-    const double x = eps * Imax;
-    segT = {kTauScale * x * x};
+
+  // ---- exact thresholds of the outputs
+  if (mode == 0) {
+    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Ms, Mo);
+    if ((st = seg_sums(c->d_w.p, Io, Mo, nullptr))) return st;
+    for (int s = 0; s < nseg; ++s) segT[s] = tau_of(hseg[3 * s], hseg[3 * s + 1]);
+  } else if (mode == 1) {
+    double imax = 0.0, emax = 0.0;
+    if ((st = absmax(Is, Ms, ngrid, &imax, &emax))) return st;
+    const double x = eps * imax;
+    segT[0] = tau_scale * x * x;
   } else {
-    segT = {0.0};
+    segT[0] = 0.0;
   }
-  if (dT.reserve(segT.size())) {
-    rel();
-    return set_error(c, INCA_E_NOMEM, "thresholds");
+  INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
+  INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, mode, c->d_perm.p, seg_of, dT, c->d_w.p, Is, Ms, eps,
+              tau_scale, fused ? nullptr : glt, ptau);
+  INCA_CUDA(c, cudaGetLastError());
+  bool run_pass2 = true;
+  if (fused) {
+    INCA_LAUNCH(c, k_band, gblk, 256, 0, ngrid, ngroups, ptau, ptau_est, glt, stats + 12);
+    unsigned long long nband = 0;
+    INCA_CUDA(c, cudaMemcpyAsync(&nband, stats + 12, sizeof(nband), cudaMemcpyDeviceToHost, c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+    run_pass2 = nband > 0;
   }
-  INCA_CUDA(c, cudaMemcpyAsync(dT.p, segT.data(), sizeof(double) * segT.size(), cudaMemcpyHostToDevice, c->stream));
-  INCA_LAUNCH(c, k_thresholds, static_cast<unsigned>((ngroups + 7) / 8), 256, 0, ngrid, ngroups, mode, c->d_perm.p,
-              seg_of, dT.p, c->d_w.p, Is, Ms, eps, glt, ptau);
-  INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev[3], c->stream));
-  INCA_LAUNCH(c, k_pass2, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-              c->d_plo.p, wbox, gbox, glt, ptau, tab, ngrid, nsplit, stage_floats, p2, stats, errw);
-  INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev[4], c->stream));
-  INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, p2, Is);
+  INCA_CUDA(c, cudaEventRecord(ev.e[3], c->stream));
+  if (run_pass2) {
+    INCA_LAUNCH(c, k_pass2, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+                c->d_plo.p, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, tab, ngrid, nsplit, stage_floats, p2,
+                stats + 4, errw);
+    INCA_CUDA(c, cudaGetLastError());
+  }
+  INCA_CUDA(c, cudaEventRecord(ev.e[4], c->stream));
+  INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, run_pass2 ? p2 : nullptr, Is);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, c->d_ivec.p);
   INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev[5], c->stream));
-  INCA_CUDA(c, cudaEventSynchronize(ev[5]));
-  rel();
+  INCA_CUDA(c, cudaEventRecord(ev.e[5], c->stream));
+  INCA_CUDA(c, cudaEventSynchronize(ev.e[5]));
   float t12 = 0, t34 = 0, t05 = 0;
-  cudaEventElapsedTime(&t12, ev[1], ev[2]);
-  cudaEventElapsedTime(&t34, ev[3], ev[4]);
-  cudaEventElapsedTime(&t05, ev[0], ev[5]);
-  for (auto& e : ev) cudaEventDestroy(e);
-  unsigned long long hs[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);
+  cudaEventElapsedTime(&t34, ev.e[3], ev.e[4]);
+  cudaEventElapsedTime(&t05, ev.e[0], ev.e[5]);
+  unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int herr = 0;
   INCA_CUDA(c, cudaMemcpy(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost));
   INCA_CUDA(c, cudaMemcpy(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost));
   if (herr) return set_error(c, INCA_E_TIMEOUT, "inca_eval: a bounded wait for a staged quartet chunk gave up");
   c->t_total_ms = t05;
-  c->t_kernel_ms = t12;  // pass 1
-  c->t_pass2_ms = t34;
+  c->t_kernel_ms = t12;  // the pass over all terms
+  c->t_pass2_ms = t34;   // the correction pass (0 when the one-pass form needed none)
   c->t_kernel_launches = 1;
-  c->t_launches = 9;
-  c->pairs_fp32 = static_cast<int64_t>(hs[0]);
-  c->pairs_fp64 = static_cast<int64_t>(hs[1]);
-  c->pairs_skip = static_cast<int64_t>(hs[2]);
-  c->corrected_points = static_cast<int64_t>(hs[3]) * 32;
+  c->t_launches = static_cast<int>(c->launches - launches0);
+  if (fused) {
+    // one-pass kernel: live pairs, warp rounds of corrections (one corrected term per active
+    // lane), exact corrected-term count; correction pass: candidate pairs and corrected terms
+    // in warps of 32 points
+    c->pairs_fp32 = static_cast<int64_t>(hs[0]);
+    c->pairs_fp64 = static_cast<int64_t>(hs[1]) + static_cast<int64_t>(hs[5]);
+    c->pairs_skip = static_cast<int64_t>(hs[2]);
+    c->corrected_points = static_cast<int64_t>(hs[3]) + 32 * static_cast<int64_t>(hs[7]);
+  } else {
+    c->pairs_fp32 = static_cast<int64_t>(hs[4]);
+    c->pairs_fp64 = static_cast<int64_t>(hs[5]);
+    c->pairs_skip = static_cast<int64_t>(hs[2]);
+    c->corrected_points = static_cast<int64_t>(hs[7]) * 32;
+  }
   return INCA_OK;
 }
 

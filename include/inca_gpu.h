@@ -157,9 +157,11 @@ int inca_centercalc(int32_t natoms, const int32_t* an, const double* cartes, int
 int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
                           int32_t* kernel_launches, int32_t* launches);
 
-/* Work split of the last INCA_MIXED evaluation, in (quartet, 128-point tile) pairs: kept in
- * FP32, examined for corrections (the precise tier), skipped (bound below 2^-120); and the
- * number of (quartet, point) terms re-evaluated in double-float arithmetic (counted in warps
+/* Work split of the last INCA_MIXED evaluation, in (quartet, 128-point tile) pairs: evaluated
+ * in FP32, examined for corrections (the precise tier; in the one-pass form used on grids of
+ * 16 384 points or more, the warp rounds of inline corrections plus the pairs examined by a
+ * correction pass, if one ran), skipped (bound below 2^-120); and the number of (quartet,
+ * point) terms re-evaluated in double-float arithmetic (a correction pass counts them in warps
  * of 32 points). The FP64 form reports zeros. Pointers may be NULL. */
 int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* precise_pairs,
                          int64_t* skipped_pairs, int64_t* corrected_terms);

@@ -1,0 +1,90 @@
+"""One-pass mixed evaluation (grids of at least 16 384 points) against the FP64 GPU form.
+
+The FP64 GPU form is checked against the oracle at 1e-12 in test_gpu_parity.py and serves as
+the full-size oracle here. Tolerances: 1e-8 relative on each I(s), 1e-10 relative on the radial
+integral, 1e-8 of max|I| on the vector cube. The threshold estimates are also forced to both
+extremes (INCA_EST_SAFETY): 0 corrects every term in the one pass; 1e6 leaves the corrections
+to the correction pass, which must then run and still meet the tolerance.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+THRESH = 1e-12
+SCAN = ([0.0], [10.0], [0.05], [590])
+
+
+@pytest.fixture(scope="module")
+def ctx(ch4):
+    from inca_parallel_gb300 import build
+    build.build()
+    from inca_parallel_gb300 import Context
+    c = Context(0)
+    c.set_primitives(ch4["alpha"], ch4["tmn"], ch4["xyz"])
+    c.set_quartets(ch4["ijkl"], ch4["v"])
+    c.prepare(THRESH)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def scan_fp64(ctx):
+    nr, ng = ctx.grid_scan(*SCAN)
+    assert ng == 62390
+    ctx.eval(mode=0)
+    return ctx.radial_plot()[1]
+
+
+def _scan_mixed(ctx):
+    ctx.grid_scan(*SCAN)
+    ctx.eval(mode=1, tol=1e-8)
+    return ctx.radial_plot()[1]
+
+
+def test_radial_plot_one_pass(ctx, scan_fp64):
+    I = _scan_mixed(ctx)
+    rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+    assert rel.max() <= 1e-8, rel.max()
+    assert ctx.stats()["corrected_terms"] > 0
+
+
+@pytest.mark.parametrize("safety", ["0", "1e6"])
+def test_estimate_extremes(ctx, scan_fp64, monkeypatch, safety):
+    monkeypatch.setenv("INCA_EST_SAFETY", safety)
+    I = _scan_mixed(ctx)
+    rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+    assert rel.max() <= 1e-8, rel.max()
+    if safety == "1e6":
+        assert ctx.phases()["pass2_ms"] > 0.0
+        assert ctx.stats()["precise_pairs"] > 0
+
+
+def test_one_pass_deterministic(ctx):
+    a = _scan_mixed(ctx)
+    b = _scan_mixed(ctx)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_radial_integral_one_pass(ctx, ch4):
+    cent, Ps, alf = O.centercalc(ch4["an"], ch4["cartes"], nohydro=False)
+    nq = len(Ps)
+    _, _, ng = ctx.grid_radial([50] * nq, [110] * nq, alf, cent, Ps)
+    assert ng >= 16384
+    ctx.eval(mode=0)
+    ref, vref, _, _ = ctx.radial_integral()
+    ctx.eval(mode=1, tol=1e-10)
+    tot, vee, _, _ = ctx.radial_integral()
+    assert abs(tot - ref) <= 1e-10 * abs(ref), (tot, ref)
+    assert abs(vee - vref) <= 1e-10 * abs(vref), (vee, vref)
+    # sum rule N(N-1)/2 = 45 up to the grid's own quadrature error
+    assert abs(tot - 45.0) < 0.1
+
+
+def test_cube_one_pass(ctx):
+    ctx.grid_cube([0.0, 0.0, 0.0], [0.15, 0.15, 0.15], [32, 32, 32])
+    ref = ctx.eval(mode=0)
+    I = ctx.eval(mode=1, tol=1e-8)
+    assert np.abs(I - ref).max() <= 1e-8 * np.abs(ref).max()
