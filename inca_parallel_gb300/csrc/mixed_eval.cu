@@ -67,6 +67,9 @@ constexpr int64_t kFuseMinPoints = 16384;
 constexpr int64_t kSampleStride = 16;
 constexpr double kEstSafety = 0.5;
 constexpr double kCubeMargin = 2.0;
+// Share of the tolerance given to terms left out of the one-pass form (their bounds over the
+// tile sum to at most this share of eps |O|, checked after the pass).
+constexpr double kDropFrac = 0.05;
 constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kExpTab = 256;             // 2^(j/256), j = -128..128
 constexpr int kFold = 8;                 // chunks between FP64 folds
@@ -143,50 +146,20 @@ __device__ __forceinline__ ChunkRef chunk_ref(const WorkChunk* chunks, const Cla
 }
 
 // ---------------------------------------------------------------- FP32 term (both passes)
-template <int NP, int L>
-__device__ __forceinline__ void horner_pts(const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
-#pragma unroll
-  for (int p = 0; p < NP; ++p) v[p] = C[0];
-#pragma unroll
-  for (int m = 1; m <= L; ++m) {
-    const float c = C[m];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], u[p], c);
-  }
-}
-
-template <int NP, int L>
-__device__ __forceinline__ void horner_abs_pts(const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
-#pragma unroll
-  for (int p = 0; p < NP; ++p) v[p] = fabsf(C[0]);
-#pragma unroll
-  for (int m = 1; m <= L; ++m) {
-    const float c = fabsf(C[m]);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], fabsf(u[p]), c);
-  }
-}
-
-// Polynomial of a class-uniform (warp-uniform) degree: one indirect branch per quartet.
+// Polynomial of a class-uniform (warp-uniform) degree L at NP points, Horner with FMA; a loop
+// over the degree (not unrolled) keeps the kernel's code small enough for the instruction cache.
 // kAbs: sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error.
 template <int NP, bool kAbs>
 __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
-#define INCA_POLY_CASE(n)                      \
-  case n:                                      \
-    if (kAbs) horner_abs_pts<NP, n>(C, u, v);  \
-    else horner_pts<NP, n>(C, u, v);           \
-    break;
-  switch (L) {
-    INCA_POLY_CASE(0) INCA_POLY_CASE(1) INCA_POLY_CASE(2) INCA_POLY_CASE(3) INCA_POLY_CASE(4)
-    INCA_POLY_CASE(5) INCA_POLY_CASE(6) INCA_POLY_CASE(7) INCA_POLY_CASE(8) INCA_POLY_CASE(9)
-    INCA_POLY_CASE(10) INCA_POLY_CASE(11) INCA_POLY_CASE(12) INCA_POLY_CASE(13) INCA_POLY_CASE(14)
-    INCA_POLY_CASE(15)
-    default:
-      if (kAbs) horner_abs_pts<NP, 16>(C, u, v);
-      else horner_pts<NP, 16>(C, u, v);
-      break;
+  const float c0 = kAbs ? fabsf(C[0]) : C[0];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) v[p] = c0;
+#pragma unroll 1
+  for (int m = 1; m <= L; ++m) {
+    const float c = kAbs ? fabsf(C[m]) : C[m];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], kAbs ? fabsf(u[p]) : u[p], c);
   }
-#undef INCA_POLY_CASE
 }
 
 // The FP32 term of quartet record R at NP points, and a bound e on its rounding error:
@@ -365,44 +338,85 @@ __device__ __forceinline__ f2 df_exp2(f2 y, const float2* __restrict__ tab) {
   return {__fmul_rn(r.hi, sc), __fmul_rn(r.lo, sc)};
 }
 
-// The double-float term of record R at one point (r_hi + r_lo per dimension).
-__device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry, float rz,
-                                   float lx, float ly, float lz, const float2* __restrict__ tab) {
-  const int L[3] = {L0, L1, L2};
-  const int nc = L0 + L1 + L2 + 3;
-  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
-  const float s_hi = R[0], s_lo = R[1];
-  f2 u[3];
+// The double-float terms of N records of one class at one point (r_hi + r_lo per dimension);
+// the N evaluations are independent, so N > 1 gives the scheduler independent chains.
+template <int N>
+__device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int L[3], const float (&rh)[3],
+                                          const float (&rl)[3], const float2* __restrict__ tab, f2 (&out)[N]) {
+  const int nc = L[0] + L[1] + L[2] + 3;
+  f2 u[N][3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const float p = __fmul_rn(s_hi, rh[d]);
-    float e = __fmaf_rn(s_hi, rh[d], -p);
-    const f2 t = two_sum(p, R[2 + d]);
-    e = __fadd_rn(e, t.lo);
-    e = __fmaf_rn(s_hi, rl[d], e);
-    e = __fmaf_rn(s_lo, rh[d], e);
-    e = __fadd_rn(e, R[5 + d]);
-    u[d] = fast_two_sum(t.hi, e);  // |e| << |t.hi| except near u = 0, where it is harmless
+  for (int n = 0; n < N; ++n) {
+    const float s_hi = R[n][0], s_lo = R[n][1];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float p = __fmul_rn(s_hi, rh[d]);
+      float e = __fmaf_rn(s_hi, rh[d], -p);
+      const f2 t = two_sum(p, R[n][2 + d]);
+      e = __fadd_rn(e, t.lo);
+      e = __fmaf_rn(s_hi, rl[d], e);
+      e = __fmaf_rn(s_lo, rh[d], e);
+      e = __fadd_rn(e, R[n][5 + d]);
+      u[n][d] = fast_two_sum(t.hi, e);  // |e| << |t.hi| except near u = 0, where it is harmless
+    }
   }
-  f2 y = df_add(df_add(df_sqr(u[0]), df_sqr(u[1])), df_sqr(u[2]));
-  y.hi = -y.hi;
-  y.lo = -y.lo;
-  f2 t = df_exp2(y, tab);
-  const float* C = R + 12;
+  f2 t[N];
+#pragma unroll
+  for (int n = 0; n < N; ++n) {
+    f2 y = df_add(df_add(df_sqr(u[n][0]), df_sqr(u[n][1])), df_sqr(u[n][2]));
+    y.hi = -y.hi;
+    y.lo = -y.lo;
+    t[n] = df_exp2(y, tab);
+  }
   int o = 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     if (L[d] == 0) {  // normalised constant polynomial: exactly +-1
-      if (C[o] < 0.0f) t = {-t.hi, -t.lo};
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        if (R[n][12 + o] < 0.0f) t[n] = {-t[n].hi, -t[n].lo};
       o += 1;
       continue;
     }
-    f2 v = {C[o], C[o + nc]};
-    for (int m = 1; m <= L[d]; ++m) v = df_add(df_mul(v, u[d]), f2{C[o + m], C[o + m + nc]});
+    f2 v[N];
+#pragma unroll
+    for (int n = 0; n < N; ++n) v[n] = {R[n][12 + o], R[n][12 + o + nc]};
+    for (int m = 1; m <= L[d]; ++m) {
+#pragma unroll
+      for (int n = 0; n < N; ++n) v[n] = df_add(df_mul(v[n], u[n][d]), f2{R[n][12 + o + m], R[n][12 + o + m + nc]});
+    }
     o += L[d] + 1;
-    t = df_mul(t, v);
+#pragma unroll
+    for (int n = 0; n < N; ++n) t[n] = df_mul(t[n], v[n]);
   }
-  return df_mul(t, f2{R[8], R[9]});
+#pragma unroll
+  for (int n = 0; n < N; ++n) out[n] = df_mul(t[n], f2{R[n][8], R[n][9]});
+}
+
+// The double-float term of record R at one point (compact code for the correction pass).
+__device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry, float rz,
+                                   float lx, float ly, float lz, const float2* __restrict__ tab) {
+  const int L[3] = {L0, L1, L2};
+  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
+  const float* const Rs[1] = {R};
+  f2 out[1];
+  term_df_n<1>(Rs, L, rh, rl, tab, out);
+  return out[0];
+}
+
+struct f2x2 {
+  f2 a, b;
+};
+// Two double-float terms (records Ra, Rb of one class) at one point.
+__device__ __noinline__ f2x2 term_df2(const float* __restrict__ Ra, const float* __restrict__ Rb, int L0, int L1,
+                                      int L2, float rx, float ry, float rz, float lx, float ly, float lz,
+                                      const float2* __restrict__ tab) {
+  const int L[3] = {L0, L1, L2};
+  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
+  const float* const Rs[2] = {Ra, Rb};
+  f2 out[2];
+  term_df_n<2>(Rs, L, rh, rl, tab, out);
+  return {out[0], out[1]};
 }
 
 // log2 upper bound of |A'| E prod_d P_d over a box (see the file comment); *lerr gets the log2
@@ -498,8 +512,9 @@ __global__ void __launch_bounds__(32, 16)
 k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
         const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats,
-        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, double* __restrict__ part,
-        double* __restrict__ part_abs, unsigned long long* __restrict__ stats, int* __restrict__ err) {
+        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop,
+        double* __restrict__ part, double* __restrict__ part_abs, double* __restrict__ drop_mass,
+        unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
@@ -523,6 +538,10 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
   float box[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) box[k] = wtbox[wtile * 8 + k];
+  // quartets whose bound over the tile is at most 2^thr are left out; the one-pass form raises
+  // thr to the tile's drop threshold and sums the bounds it left out (dm)
+  const float thr = (kFuse && lt_drop) ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
+  float dm = 0.0f;
   double acc[kPPT];
   float sh[kPPT], sl[kPPT], sa[kPPT];
 #pragma unroll
@@ -543,7 +562,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     const float* st = S.buf[k & 1];
     const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
     const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
-    uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > kSkipLog2);
+    uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+    if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
     if (lane == 0) {
       nskip += w.count - __popc(m);
       nlive += __popc(m);
@@ -571,16 +591,22 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     if (kFuse) {
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
+        // two terms per lane and round (independent chains); a lone last term is paired with
+        // itself and the copy discarded, so the lanes of a round run the same code
         uint32_t mm = nm[p];
         while (__any_sync(0xffffffffu, mm != 0u)) {
           ++nround;
           if (mm) {
-            const int q = __ffs(mm) - 1;
+            const int qa = __ffs(mm) - 1;
             mm &= mm - 1;
-            const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p],
-                                   rl[1][p], rl[2][p], tab);
-            corr[p] = df_add(corr[p], tdf);
-            ++ncorr;
+            const bool two = mm != 0u;
+            const int qb = two ? __ffs(mm) - 1 : qa;
+            if (two) mm &= mm - 1;
+            const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], rh[0][p],
+                                    rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
+            corr[p] = df_add(corr[p], r.a);
+            if (two) corr[p] = df_add(corr[p], r.b);
+            ncorr += two ? 2 : 1;
           }
         }
       }
@@ -615,7 +641,12 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     }
   }
   if (kFuse) {
-    for (int o = 16; o > 0; o >>= 1) ncorr += __shfl_xor_sync(0xffffffffu, ncorr, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      ncorr += __shfl_xor_sync(0xffffffffu, ncorr, o);
+      dm += __shfl_xor_sync(0xffffffffu, dm, o);
+    }
+    // the FP32 sum of the left-out bounds, raised by a margin for its own rounding
+    if (lane == 0 && drop_mass) drop_mass[blockIdx.y * static_cast<int64_t>(gridDim.x) + wtile] = dm * 1.0001;
   }
   if (lane == 0) {
     atomicAdd(&stats[2], nskip);
@@ -632,9 +663,9 @@ __global__ void __launch_bounds__(32, 16)
 k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
         const float* __restrict__ wtbox, const float* __restrict__ gbox, const float* __restrict__ g_lt,
-        const float* __restrict__ pt_tau, const float* __restrict__ pt_tau_est, const float2* __restrict__ exp_tab,
-        int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part, unsigned long long* __restrict__ stats,
-        int* __restrict__ err) {
+        const float* __restrict__ pt_tau, const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop,
+        const float2* __restrict__ exp_tab, int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part,
+        unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kExpTab + 1];
@@ -654,6 +685,7 @@ k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
   float wbox[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) wbox[k] = wtbox[wtile * 8 + k];
+  const float thr = lt_drop ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
   double acc[kPPT];
   f2 corr[kPPT];
 #pragma unroll
@@ -674,9 +706,9 @@ k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
     const float* st = S.buf[k & 1];
     const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
     const float* Rq = st + lane * sg.stride32;
-    // pass 1's skip decision for this quartet (same box, same arithmetic)
+    // pass 1's skip decision for this quartet (same box, same arithmetic, same threshold)
     const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
-    const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > kSkipLog2);
+    const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
     uint32_t msub[kPPT];
     uint32_t any = 0;
 #pragma unroll
@@ -955,6 +987,27 @@ __global__ void k_seg_sums(int nseg, const int64_t* __restrict__ off, const doub
     for (int j = 0; j < 3; ++j) out[3 * seg + j] = s[j][0];
 }
 
+// log2 of the smallest per-point value of each 128-point tile (one warp per tile).
+__global__ void k_tile_min_log2(int64_t n, int64_t nwt, const float* __restrict__ pt, float* lt) {
+  const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
+  if (wt >= nwt) return;
+  const int lane = threadIdx.x & 31;
+  float t = HUGE_VALF;
+  for (int p = 0; p < kPPT; ++p) {
+    const int64_t i = wt * kWarpTile + lane + 32 * p;
+    if (i < n) t = fminf(t, pt[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
+  if (lane == 0) lt[wt] = t >= HUGE_VALF ? HUGE_VALF : (t > 0.0f ? log2f(t) : -HUGE_VALF);
+}
+
+// Per-tile values spread to the tile's points, in grid order.
+__global__ void k_tile_to_points(int64_t n, const int64_t* __restrict__ perm, const double* __restrict__ vt,
+                                 double* out) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i < n) out[perm[i]] = vt[i / kWarpTile];
+}
+
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
@@ -1100,9 +1153,9 @@ int eval_mixed(inca_ctx* c, double eps) {
   const int nseg = off.empty() ? 1 : static_cast<int>(off.size()) - 1;
 
   // scratch: pass sums and error-bound sums (nsplit x n), I~ / E~ sorted and grid order,
-  // thresholds, statistics, the exp table, segment sums
-  double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT;
-  float *glt, *ptau, *ptau_est;
+  // thresholds, left-out bound mass per tile, statistics, the exp table, segment sums
+  double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT, *dmass, *Dt, *Dpt;
+  float *glt, *ptau, *ptau_est, *ptheta, *ltdrop;
   unsigned long long *stats, *dmax;
   int* errw;
   int64_t* doff;
@@ -1118,6 +1171,11 @@ int eval_mixed(inca_ctx* c, double eps) {
     glt = cv.take<float>(ngroups);
     ptau = cv.take<float>(ngrid);
     ptau_est = cv.take<float>(fused ? ngrid : 1);
+    ptheta = cv.take<float>(fused ? ngrid : 1);
+    ltdrop = cv.take<float>(fused ? nwt : 1);
+    dmass = cv.take<double>(fused ? static_cast<size_t>(nsplit) * nwt : 1);
+    Dt = cv.take<double>(fused ? nwt : 1);
+    Dpt = cv.take<double>(fused ? ngrid : 1);
     stats = cv.take<unsigned long long>(16);
     dmax = cv.take<unsigned long long>(2);
     errw = cv.take<int>(4);
@@ -1138,6 +1196,13 @@ int eval_mixed(inca_ctx* c, double eps) {
     const double v = std::strtod(env, &end);
     if (end != env && v > 0.0 && std::isfinite(v)) tau_scale = v;
   }
+  // INCA_DROP_FRACTION overrides the share of the tolerance given to left-out terms (0: none)
+  double drop_frac = kDropFrac;
+  if (const char* env = std::getenv("INCA_DROP_FRACTION")) {
+    char* end = nullptr;
+    const double v = std::strtod(env, &end);
+    if (end != env && v >= 0.0 && v < 0.5) drop_frac = v;
+  }
   const std::vector<float2> htab = exp2_table();
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
@@ -1150,7 +1215,8 @@ int eval_mixed(inca_ctx* c, double eps) {
   const int stage_floats = kChunkMax * max_stride;
   const size_t dsmem = 128 + 2 * sizeof(float) * stage_floats;
   const unsigned gblk = static_cast<unsigned>((ngroups + 7) / 8);
-  std::vector<double> hseg(6 * nseg), segT(nseg);
+  const unsigned tblk = static_cast<unsigned>((nwt + 7) / 8);
+  std::vector<double> hseg(6 * nseg), segT(nseg), segD(nseg, 0.0);
 
   // segment sums of w I~, w E~, w (first three) and, with a second weight array, w2 (sixth)
   auto seg_sums = [&](const double* w, const double* I, const double* M, const double* w2) -> int {
@@ -1172,13 +1238,12 @@ int eval_mixed(inca_ctx* c, double eps) {
     std::memcpy(emax, &hm[1], sizeof(double));
     return INCA_OK;
   };
-  auto tau_of = [&](double O, double M) {
-    const double lo = std::max(std::fabs(O) - M, 0.0);
-    const double x = eps * lo;
-    return M > 0.0 ? tau_scale * x * x / M : HUGE_VAL;
-  };
+  // threshold of an output: 3 sigma of the uncorrected rounding errors within the absolute
+  // budget B (tolerance times a lower bound of |O|, less the left-out bound mass)
+  auto tau_of_budget = [&](double B, double M) { return M > 0.0 ? tau_scale * B * B / M : HUGE_VAL; };
 
-  // ---- threshold estimates from the grid sample (one-pass form)
+  // ---- estimates from the grid sample (one-pass form): thresholds and drop thresholds
+  bool use_drop = false;
   if (fused) {
     // INCA_EST_SAFETY overrides the factor applied to the estimated thresholds (a test and
     // tuning knob: larger values trade correction-pass work for one-pass work)
@@ -1208,11 +1273,13 @@ int eval_mixed(inca_ctx* c, double eps) {
     layout_s(cs);
     dim3 grid_s(static_cast<unsigned>(nwt_s), static_cast<unsigned>(nsplit_s));
     INCA_LAUNCH(c, k_pass1<false>, grid_s, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
-                c->d_phi_s.p, c->d_plo_s.p, c->d_wtbox_s.p, ns, nsplit_s, stage_floats, nullptr, nullptr, q1, qabs,
-                stats + 8, errw);
+                c->d_phi_s.p, c->d_plo_s.p, c->d_wtbox_s.p, ns, nsplit_s, stage_floats, nullptr, nullptr, nullptr, q1,
+                qabs, nullptr, stats + 8, errw);
     INCA_CUDA(c, cudaGetLastError());
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, q1, nullptr, Iss);
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, qabs, nullptr, Mss);
+    std::vector<double> segTheta(nseg, 0.0);
+    const double nq = static_cast<double>(std::max<int64_t>(c->nsurv, 1));
     int emode = 0;
     if (mode == 0) {
       INCA_CUDA(c, cudaMemsetAsync(Ios, 0, sizeof(double) * ngrid, c->stream));
@@ -1223,55 +1290,99 @@ int eval_mixed(inca_ctx* c, double eps) {
       for (int s = 0; s < nseg; ++s) {
         const double wsam = hseg[3 * s + 2], wtot = hseg[3 * nseg + 3 * s + 2];
         const double f = wsam > 0.0 ? wtot / wsam : 0.0;
-        const double t = tau_of(hseg[3 * s] * f, hseg[3 * s + 1] * f);
-        segT[s] = (wsam > 0.0 && hseg[3 * s + 1] > 0.0) ? safety * t : 0.0;
+        const double O = hseg[3 * s] * f, M = hseg[3 * s + 1] * f;
+        const double lo = std::max(std::fabs(O) - M, 0.0);
+        segT[s] = (wsam > 0.0 && M > 0.0) ? safety * tau_of_budget(eps * lo, M) : 0.0;
+        // drop threshold per point: theta_g = Theta / w_g with sum_g w_g nq theta_g equal to
+        // drop_frac eps |O| (half the estimate, for its sampling error)
+        const double npts = static_cast<double>(off[s + 1] - off[s]);
+        segTheta[s] = wsam > 0.0 ? 0.5 * drop_frac * eps * lo / (nq * std::max(npts, 1.0)) : 0.0;
       }
     } else {
       emode = 3;
       double imax = 0.0, emax = 0.0;
       if ((st = absmax(Iss, Mss, ns, &imax, &emax))) return st;
-      const double x = eps * imax;
-      segT[0] = emax > 0.0 ? safety * tau_scale * x * x / (kCubeMargin * emax) : 0.0;
+      segT[0] = emax > 0.0 ? safety * tau_of_budget(eps * imax, kCubeMargin * emax) : 0.0;
+      segTheta[0] = 0.5 * drop_frac * eps * imax / nq;
     }
     INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
     INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
                 nullptr, eps, tau_scale, nullptr, ptau_est);
+    use_drop = drop_frac > 0.0;
+    if (use_drop) {
+      // (pageable host copies are staged before the call returns; the stream orders the rest)
+      INCA_CUDA(c, cudaMemcpyAsync(dT, segTheta.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
+      INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
+                  nullptr, eps, tau_scale, nullptr, ptheta);
+      INCA_LAUNCH(c, k_tile_min_log2, tblk, 256, 0, ngrid, nwt, ptheta, ltdrop);
+    }
     INCA_CUDA(c, cudaGetLastError());
   }
 
-  // ---- the pass over all terms (one-pass form: with corrections above the estimates)
-  INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
   dim3 grid(static_cast<unsigned>(nwt), static_cast<unsigned>(nsplit));
-  if (fused)
-    INCA_LAUNCH(c, k_pass1<true>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                c->d_plo.p, wbox, ngrid, nsplit, stage_floats, ptau_est, tab, p1, pabs, stats, errw);
-  else
-    INCA_LAUNCH(c, k_pass1<false>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
-                c->d_phi.p, c->d_plo.p, wbox, ngrid, nsplit, stage_floats, nullptr, nullptr, p1, pabs, stats, errw);
-  INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
-  INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
-  INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, pabs, nullptr, Ms);
-  INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
+  bool run_pass2 = true;
+  for (int attempt = 0;; ++attempt) {
+    // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
+    // terms below the drop thresholds left out)
+    INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
+    if (fused)
+      INCA_LAUNCH(c, k_pass1<true>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+                  c->d_plo.p, wbox, ngrid, nsplit, stage_floats, ptau_est, tab, use_drop ? ltdrop : nullptr, p1, pabs,
+                  dmass, stats, errw);
+    else
+      INCA_LAUNCH(c, k_pass1<false>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
+                  c->d_phi.p, c->d_plo.p, wbox, ngrid, nsplit, stage_floats, nullptr, nullptr, nullptr, p1, pabs,
+                  nullptr, stats, errw);
+    INCA_CUDA(c, cudaGetLastError());
+    INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
+    INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
+    INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, pabs, nullptr, Ms);
+    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
+    if (use_drop) {
+      INCA_LAUNCH(c, k_sum_splits, nblk(nwt), 256, 0, nwt, nsplit, dmass, nullptr, Dt);
+      INCA_LAUNCH(c, k_tile_to_points, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Dt, Dpt);
+    }
 
-  // ---- exact thresholds of the outputs
-  if (mode == 0) {
-    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Ms, Mo);
-    if ((st = seg_sums(c->d_w.p, Io, Mo, nullptr))) return st;
-    for (int s = 0; s < nseg; ++s) segT[s] = tau_of(hseg[3 * s], hseg[3 * s + 1]);
-  } else if (mode == 1) {
-    double imax = 0.0, emax = 0.0;
-    if ((st = absmax(Is, Ms, ngrid, &imax, &emax))) return st;
-    const double x = eps * imax;
-    segT[0] = tau_scale * x * x;
-  } else {
-    segT[0] = 0.0;
+    // ---- exact thresholds of the outputs
+    bool retry = false;
+    if (mode == 0) {
+      INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Ms, Mo);
+      if (use_drop) {  // sum_g w_g D_g per segment (first of the three sums k_seg_sums writes)
+        INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, c->d_w.p, Dpt, Dpt, dout + 3 * nseg);
+        INCA_CUDA(c, cudaMemcpyAsync(hseg.data() + 3 * nseg, dout + 3 * nseg, sizeof(double) * 3 * nseg,
+                                     cudaMemcpyDeviceToHost, c->stream));
+        INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int s = 0; s < nseg; ++s) segD[s] = hseg[3 * nseg + 3 * s];
+      }
+      if ((st = seg_sums(c->d_w.p, Io, Mo, nullptr))) return st;
+      for (int s = 0; s < nseg; ++s) {
+        const double D = use_drop ? segD[s] : 0.0;
+        const double lo = std::max(std::fabs(hseg[3 * s]) - hseg[3 * s + 1] - D, 0.0);
+        const double B = eps * lo - D;
+        if (use_drop && B < 0.5 * eps * lo) retry = true;
+        segT[s] = tau_of_budget(std::max(B, 0.0), hseg[3 * s + 1]);
+      }
+    } else if (mode == 1) {
+      double imax = 0.0, emax = 0.0, dmx = 0.0, unused = 0.0;
+      if ((st = absmax(Is, Ms, ngrid, &imax, &emax))) return st;
+      if (use_drop && (st = absmax(Dt, Dt, nwt, &dmx, &unused))) return st;
+      const double B = eps * imax - dmx;
+      if (use_drop && B < 0.5 * eps * imax) retry = true;
+      segT[0] = tau_scale * std::max(B, 0.0) * std::max(B, 0.0);
+    } else {
+      segT[0] = 0.0;
+    }
+    if (retry && attempt == 0) {  // too much was left out: once more without leaving terms out
+      use_drop = false;
+      INCA_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), c->stream));
+      continue;
+    }
+    break;
   }
   INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
   INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, mode, c->d_perm.p, seg_of, dT, c->d_w.p, Is, Ms, eps,
               tau_scale, fused ? nullptr : glt, ptau);
   INCA_CUDA(c, cudaGetLastError());
-  bool run_pass2 = true;
   if (fused) {
     INCA_LAUNCH(c, k_band, gblk, 256, 0, ngrid, ngroups, ptau, ptau_est, glt, stats + 12);
     unsigned long long nband = 0;
@@ -1282,8 +1393,8 @@ int eval_mixed(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaEventRecord(ev.e[3], c->stream));
   if (run_pass2) {
     INCA_LAUNCH(c, k_pass2, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                c->d_plo.p, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, tab, ngrid, nsplit, stage_floats, p2,
-                stats + 4, errw);
+                c->d_plo.p, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, use_drop ? ltdrop : nullptr, tab, ngrid,
+                nsplit, stage_floats, p2, stats + 4, errw);
     INCA_CUDA(c, cudaGetLastError());
   }
   INCA_CUDA(c, cudaEventRecord(ev.e[4], c->stream));
