@@ -57,6 +57,7 @@ SIGNATURES = {
     "inca_get_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
+    "inca_fp32_fma_peak": (ctypes.c_int, [VP, DP]),
     "inca_eval_records_noalloc": (ctypes.c_int, [ctypes.c_int64, VP, VP, VP, VP, VP, ctypes.c_int64, VP, VP, VP]),
 }
 
@@ -275,6 +276,12 @@ class Context:
         self._check(self.lib.inca_last_eval_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                                   ctypes.byref(d)))
         return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value, "corrected_terms": d.value}
+
+    def fp32_peak_tflops(self):
+        """Measured FP32 FMA throughput of the context's GPU (TFLOP/s)."""
+        t = ctypes.c_double()
+        self._check(self.lib.inca_fp32_fma_peak(self.h, ctypes.byref(t)))
+        return t.value
 
     def phases(self):
         a, b = ctypes.c_double(), ctypes.c_double()

@@ -29,6 +29,7 @@ UNITS = {
     "mixed_eval.cu": [],
     "grid_build.cu": ["-fmad=false"],
     "noalloc_eval.cu": [],
+    "peak_probe.cu": [],
     "host_tables.cpp": [],
 }
 DRIVER_SRC = os.path.join(CSRC, "driver", "inca_main.cpp")

@@ -74,6 +74,14 @@ constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kExpTab = 256;             // 2^(j/256), j = -128..128
 constexpr int kFold = 8;                 // chunks between FP64 folds
 constexpr int kWaitLimit = 1 << 22;      // bounded mbarrier waits
+// Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
+// whether inline corrections evaluate two terms per lane and round.
+#ifndef INCA_PASS_CTAS_PER_SM
+#define INCA_PASS_CTAS_PER_SM 16
+#endif
+#ifndef INCA_DF_PAIRS
+#define INCA_DF_PAIRS 1
+#endif
 
 // 2^y for y <= 0 in FP32 without systematic bias: y = n + f (n = rint(y), |f| <= 1/2),
 // 2^f by a degree-7 polynomial (Chebyshev interpolation of 2^x on [-1/2, 1/2], relative
@@ -508,7 +516,7 @@ __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chun
 //   terms in double-float, each lane working down its own list (the chunk is class-uniform,
 //   so the lanes run the same instruction sequence on different quartets).
 template <bool kFuse>
-__global__ void __launch_bounds__(32, 16)
+__global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
         const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
         const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats,
@@ -596,7 +604,14 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
         uint32_t mm = nm[p];
         while (__any_sync(0xffffffffu, mm != 0u)) {
           ++nround;
-          if (mm) {
+          if (!INCA_DF_PAIRS && mm) {
+            const int q = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p],
+                                   rl[1][p], rl[2][p], tab);
+            corr[p] = df_add(corr[p], tdf);
+            ++ncorr;
+          } else if (mm) {
             const int qa = __ffs(mm) - 1;
             mm &= mm - 1;
             const bool two = mm != 0u;
@@ -1130,7 +1145,7 @@ int eval_mixed(inca_ctx* c, double eps) {
   if (st) return st;
   const int64_t nwt = (ngrid + kWarpTile - 1) / kWarpTile;
   const int64_t ngroups = nwt * kPPT;
-  const int nsplit = choose_splits(nwt, nchunks, c->num_sms, 16);
+  const int nsplit = choose_splits(nwt, nchunks, c->num_sms, INCA_PASS_CTAS_PER_SM);
   const float* wbox = c->d_wtbox.p;
   const float* gbox = c->d_wtbox.p + 8 * nwt;
 
@@ -1255,7 +1270,7 @@ int eval_mixed(inca_ctx* c, double eps) {
     }
     const int64_t ns = c->nsample;
     const int64_t nwt_s = (ns + kWarpTile - 1) / kWarpTile;
-    const int nsplit_s = choose_splits(nwt_s, nchunks, c->num_sms, 16);
+    const int nsplit_s = choose_splits(nwt_s, nchunks, c->num_sms, INCA_PASS_CTAS_PER_SM);
     double *q1, *qabs, *Iss, *Mss, *Ios, *Mos, *ws;
     auto layout_s = [&](Carve& cs) {
       q1 = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);

@@ -178,6 +178,11 @@ int inca_get_stream(inca_ctx* ctx, void** stream);
  * (library kernels such as CUB sorts are not counted). */
 int inca_kernel_launches(inca_ctx* ctx, int64_t* count);
 
+/* Measured FP32 FMA throughput of the context's GPU in TFLOP/s (2 flops per FMA; a short
+ * microbenchmark on the context's stream). Diagnostic with no counterpart in the reference:
+ * the roofline denominator of the evaluation kernels, which are bound by the FP32 pipe. */
+int inca_fp32_fma_peak(inca_ctx* ctx, double* tflops);
+
 /* ---------------------------------------------------------------------------------------
  * Evaluation without allocation. No counterpart in the reference (the Fortran program
  * allocates its work arrays itself); this entry point exists for callers that must not
