@@ -73,6 +73,9 @@ constexpr double kDropFrac = 0.05;
 constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kExpTab = 256;             // 2^(j/256), j = -128..128
 constexpr int kFold = 8;                 // chunks between FP64 folds
+// |u_d| limit for the polynomial factors: 2^(-u^2 + ks) is zero beyond sqrt(126 + ks) < 64
+// for every representable A' scale ks used here, and 64^16 stays finite in FP32
+constexpr float kUClamp = 64.0f;
 constexpr int kWaitLimit = 1 << 22;      // bounded mbarrier waits
 // Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
 // whether inline corrections evaluate two terms per lane and round.
@@ -88,7 +91,8 @@ constexpr int kWaitLimit = 1 << 22;      // bounded mbarrier waits
 // approximation error 3.2e-9) evaluated by FMA Horner (<= 1.1 ulp), times 2^n built from the
 // exponent bits (exact; 0 below 2^-126). The hardware ex2.approx was measured biased by
 // -5e-8 relative on this range, which the error model of the correction pass cannot absorb.
-__device__ __forceinline__ float exp2_fp32(float y) {
+// ks: an integer power of two applied exactly in the final scaling (2^(y + ks)).
+__device__ __forceinline__ float exp2_fp32(float y, int ks) {
   const float n = rintf(y);
   const float f = __fsub_rn(y, n);
   float p = 1.5303699910873547e-05f;
@@ -99,7 +103,9 @@ __device__ __forceinline__ float exp2_fp32(float y) {
   p = __fmaf_rn(p, f, 0.24022650718688965f);
   p = __fmaf_rn(p, f, 0.6931471824645996f);
   p = __fmaf_rn(p, f, 1.0f);
-  const int e = max(static_cast<int>(n) + 127, 0);
+  // n is clamped in FP32 before the integer conversion (an out-of-range conversion has no
+  // defined result); below -1000 the scale is zero for any ks used here
+  const int e = min(max(static_cast<int>(fmaxf(n, -1000.0f)) + ks + 127, 0), 254);
   return __fmul_rn(p, __int_as_float(e << 23));
 }
 
@@ -180,6 +186,7 @@ template <int NP, bool kErr>
 __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
                                         const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
   const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
+  const int ks = static_cast<int>(R[11]);
   float u[3][NP];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -198,8 +205,16 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
     y = __fmaf_rn(-u[1][p], u[1][p], y);
     y = __fmaf_rn(-u[2][p], u[2][p], y);
     Y[p] = y;
-    E[p] = exp2_fp32(y);
+    E[p] = exp2_fp32(y, ks);
   }
+  // the polynomials see u clamped to +-kUClamp: wherever E is non-zero |u_d| is far below it,
+  // and far points (E = 0) cannot overflow the polynomial into inf (0 * inf = NaN)
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) {
+#pragma unroll
+      for (int p = 0; p < NP; ++p) u[d][p] = fminf(fmaxf(u[d][p], -kUClamp), kUClamp);
+    }
   const float* Cx = R + 12;
   const float* Cy = Cx + L[0] + 1;
   const float* Cz = Cy + L[1] + 1;
@@ -257,6 +272,7 @@ __device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int
   const int L[3] = {L0, L1, L2};
   const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
   const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
+  const int ks = static_cast<int>(R[11]);
   float u[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -267,7 +283,10 @@ __device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int
   float y = __fmul_rn(-u[0], u[0]);
   y = __fmaf_rn(-u[1], u[1], y);
   y = __fmaf_rn(-u[2], u[2], y);
-  const float E = exp2_fp32(y);
+  const float E = exp2_fp32(y, ks);
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) u[d] = fminf(fmaxf(u[d], -kUClamp), kUClamp);
   const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L0 + L1 + L2));
   const float aA = 5.9604645e-08f * fabsf(A_hi);
   float P = E, Pe = __fmul_rn(E, __fmaf_rn(fabsf(y), 3.0f * aA, k0 * fabsf(A_hi)));
@@ -322,9 +341,9 @@ __device__ __forceinline__ f2 df_sqr(f2 x) {
 
 // 2^y in double-float for y <= 0: y = n + j/256 + g, |g| <= 1/512;
 // 2^g = e^x, x = g ln2 (double-float), e^x = 1 + x + x^2/2 + x^3/6 + x^4/24 (tail in FP32).
-__device__ __forceinline__ f2 df_exp2(f2 y, const float2* __restrict__ tab) {
-  if (y.hi < -125.0f) return {0.0f, 0.0f};
+__device__ __forceinline__ f2 df_exp2(f2 y, int ks, const float2* __restrict__ tab) {
   const float n = rintf(y.hi);
+  if (n + static_cast<float>(ks) < -125.0f) return {0.0f, 0.0f};  // compared in FP32: n may be huge
   const float f = __fsub_rn(y.hi, n);  // exact
   const float j = rintf(__fmul_rn(f, 256.0f));
   const float g = __fsub_rn(f, __fmul_rn(j, 0.00390625f));  // exact
@@ -342,7 +361,7 @@ __device__ __forceinline__ f2 df_exp2(f2 y, const float2* __restrict__ tab) {
   const f2 ex = fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, q)));
   const float2 T = tab[static_cast<int>(j) + kExpTab / 2];
   const f2 r = df_mul({T.x, T.y}, ex);
-  const float sc = __int_as_float((static_cast<int>(n) + 127) << 23);  // 2^n, n >= -125
+  const float sc = __int_as_float(min(static_cast<int>(n) + ks + 127, 254) << 23);  // 2^(n + ks)
   return {__fmul_rn(r.hi, sc), __fmul_rn(r.lo, sc)};
 }
 
@@ -374,7 +393,10 @@ __device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int 
     f2 y = df_add(df_add(df_sqr(u[n][0]), df_sqr(u[n][1])), df_sqr(u[n][2]));
     y.hi = -y.hi;
     y.lo = -y.lo;
-    t[n] = df_exp2(y, tab);
+    t[n] = df_exp2(y, static_cast<int>(R[n][11]), tab);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (fabsf(u[n][d].hi) > kUClamp) u[n][d] = {copysignf(kUClamp, u[n][d].hi), 0.0f};
   }
   int o = 0;
 #pragma unroll

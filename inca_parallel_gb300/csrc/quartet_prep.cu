@@ -348,9 +348,13 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
     r32[2 + d] = b_hi;
     r32[5 + d] = static_cast<float>(b - static_cast<double>(b_hi));
   }
-  const float A_hi = static_cast<float>(Aprime);
+  // A' = m 2^k with |m| in [0.5, 1): m as an FP32 pair, k applied exactly in the exponent
+  // scaling of the evaluation's exp2 (A' itself can exceed the FP32 range for tight d shells)
+  int kA = 0;
+  const double mA = Aprime != 0.0 ? frexp(Aprime, &kA) : 0.0;
+  const float A_hi = static_cast<float>(mA);
   r32[8] = A_hi;
-  r32[9] = static_cast<float>(Aprime - static_cast<double>(A_hi));
+  r32[9] = static_cast<float>(mA - static_cast<double>(A_hi));
   // log2 of |A'| prod_d sum_k |Cn_dk|: the tile bounds of the mixed evaluation start from it
   double la = log2(fabs(Aprime));
   for (int d = 0; d < 3; ++d) {
@@ -359,7 +363,7 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
     la += log2(sd);
   }
   r32[10] = static_cast<float>(la);
-  r32[11] = 0.0f;
+  r32[11] = static_cast<float>(kA);
   const int nc = rec.L[0] + rec.L[1] + rec.L[2] + 3;
   o = 12;
   for (int d = 0; d < 3; ++d)
