@@ -93,6 +93,8 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_perm_s.release();
   c->d_wtbox_s.release();
   c->d_scratch_s.release();
+  c->d_tiles.release();
+  c->d_tiles_s.release();
   cudaStreamDestroy(c->stream);
   delete c;
   return INCA_OK;

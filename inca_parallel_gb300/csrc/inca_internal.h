@@ -69,6 +69,19 @@ struct WorkChunk {
   int64_t rec;  // first class-sorted survivor index
 };
 
+// A tile of up to 128 points of the sorted grid (consecutive), and the molecule whose
+// quartet chunks it is evaluated against (index into the per-molecule chunk ranges).
+struct TileInfo {
+  int64_t start;
+  int count;
+  int mol;
+};
+
+// The chunk range [begin, end) of one molecule.
+struct ChunkRange {
+  int begin, end;
+};
+
 enum GridKind { GRID_NONE = 0, GRID_RADIAL = 1, GRID_SCAN = 2, GRID_CUBE = 3, GRID_POINTS = 4 };
 
 }  // namespace inca
@@ -128,12 +141,16 @@ struct inca_ctx {
   inca::DevBuf<float4> d_phi, d_plo;  // FP32 hi / lo parts of the sorted points
   inca::DevBuf<int64_t> d_perm;       // sorted position -> grid index
   inca::DevBuf<float> d_wtbox;        // per 128-point warp tile: lo[3], hi[3], 2 pad
+  inca::DevBuf<inca::TileInfo> d_tiles;  // tiles of the sorted grid
+  int64_t ntiles = 0;
   // the same for a strided sample of the grid (threshold estimates of the one-pass form)
   int64_t sample_version = -1;
   int64_t nsample = 0;
   inca::DevBuf<float4> d_phi_s, d_plo_s;
   inca::DevBuf<int64_t> d_perm_s;
   inca::DevBuf<float> d_wtbox_s;
+  inca::DevBuf<inca::TileInfo> d_tiles_s;
+  int64_t ntiles_s = 0;
   inca::DevBuf<unsigned char> d_scratch_s;
 
   // scratch

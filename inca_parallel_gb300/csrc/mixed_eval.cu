@@ -77,6 +77,7 @@ constexpr int kFold = 8;                 // chunks between FP64 folds
 // for every representable A' scale ks used here, and 64^16 stays finite in FP32
 constexpr float kUClamp = 64.0f;
 constexpr int kWaitLimit = 1 << 22;      // bounded mbarrier waits
+constexpr int kItemsPerCta = 12;         // persistent passes: work items per resident CTA
 // Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
 // whether inline corrections evaluate two terms per lane and round.
 #ifndef INCA_PASS_CTAS_PER_SM
@@ -471,15 +472,15 @@ __device__ __forceinline__ float log2_bound(const float* __restrict__ R, const i
 }
 
 __device__ __forceinline__ void load_points(const float4* __restrict__ phi, const float4* __restrict__ plo,
-                                            int64_t base, int lane, int64_t ngrid, float (&rh)[3][kPPT],
+                                            const TileInfo& T, int lane, float (&rh)[3][kPPT],
                                             float (&rl)[3][kPPT]) {
 #pragma unroll
   for (int p = 0; p < kPPT; ++p) {
-    const int64_t i = base + lane + 32 * p;
+    const int j = lane + 32 * p;
     float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-    if (i < ngrid) {
-      h = phi[i];
-      l = plo[i];
+    if (j < T.count) {
+      h = phi[T.start + j];
+      l = plo[T.start + j];
     }
     rh[0][p] = h.x; rh[1][p] = h.y; rh[2][p] = h.z;
     rl[0][p] = l.x; rl[1][p] = l.y; rl[2][p] = l.z;
@@ -500,19 +501,31 @@ __device__ __forceinline__ Stage stage_view(unsigned char* dsm, int floats) {
   return S;
 }
 
-// Set up the barriers and start the first chunk's copy (lane 0).
-__device__ __forceinline__ void stage_begin(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
-                                            const float* rec32, int first, int nchunks) {
+// Set up the two barriers (once per CTA; they then serve every work item of the CTA).
+__device__ __forceinline__ void stage_init(const Stage& S) {
   if (threadIdx.x == 0) {
     mbar_init(&S.bar[0]);
     mbar_init(&S.bar[1]);
     fence_mbar_init();
   }
   __syncwarp();
-  if (threadIdx.x == 0 && first < nchunks) {
-    const ChunkRef r = chunk_ref(chunks, segs, rec32, first);
-    bulk_load(S.buf[0], r.src, r.bytes, &S.bar[0]);
+}
+
+// Start the copy of an item's first chunk (global chunk counter k) into buffer k & 1.
+__device__ __forceinline__ void stage_first(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
+                                            const float* rec32, int k, int ch) {
+  if (threadIdx.x == 0) {
+    fence_proxy_async();  // earlier generic-proxy reads of that buffer are done (warp-synchronous)
+    const ChunkRef r = chunk_ref(chunks, segs, rec32, ch);
+    bulk_load(S.buf[k & 1], r.src, r.bytes, &S.bar[k & 1]);
   }
+}
+
+// Next work item of a persistent CTA: (tile, split) pairs, taken from a device counter.
+__device__ __forceinline__ int64_t next_item(unsigned long long* work) {
+  unsigned long long it = 0;
+  if (threadIdx.x == 0) it = atomicAdd(work, 1ull);
+  return static_cast<int64_t>(__shfl_sync(0xffffffffu, it, 0));
 }
 
 // Before working on chunk k: start the copy of the next chunk into the other buffer, then wait
@@ -539,152 +552,166 @@ __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chun
 //   so the lanes run the same instruction sequence on different quartets).
 template <bool kFuse>
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
-k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
-        const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
-        const float* __restrict__ wtbox, int64_t ngrid, int nsplit, int stage_floats,
-        const float* __restrict__ pt_tau, const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop,
-        double* __restrict__ part, double* __restrict__ part_abs, double* __restrict__ drop_mass,
+k_pass1(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol_chunks,
+        const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
+        const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
+        int64_t ntiles, int nsplit, int64_t ngrid, int stage_floats, const float* __restrict__ pt_tau,
+        const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop, double* __restrict__ part,
+        double* __restrict__ part_abs, double* __restrict__ drop_mass, unsigned long long* __restrict__ work,
         unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
   const int lane = threadIdx.x;
-  const int64_t wtile = blockIdx.x;
-  const int64_t base = wtile * kWarpTile;
-  stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
-  float rh[3][kPPT], rl[3][kPPT];
-  load_points(phi, plo, base, lane, ngrid, rh, rl);
-  float tau[kPPT];
-  f2 corr[kPPT];
-  if (kFuse) {
+  if (kFuse)
     for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
-#pragma unroll
-    for (int p = 0; p < kPPT; ++p) {
-      const int64_t i = base + lane + 32 * p;
-      tau[p] = i < ngrid ? pt_tau[i] : HUGE_VALF;
-      corr[p] = {0.0f, 0.0f};
-    }
-  }
-  float box[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) box[k] = wtbox[wtile * 8 + k];
-  // quartets whose bound over the tile is at most 2^thr are left out; the one-pass form raises
-  // thr to the tile's drop threshold and sums the bounds it left out (dm)
-  const float thr = (kFuse && lt_drop) ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
-  float dm = 0.0f;
-  double acc[kPPT];
-  float sh[kPPT], sl[kPPT], sa[kPPT];
-#pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    acc[p] = 0.0;
-    sh[p] = sl[p] = sa[p] = 0.0f;
-  }
-  __syncwarp();
+  stage_init(S);
   unsigned long long nskip = 0, nlive = 0, ncorr = 0, nround = 0;
-  int nfold = 0, k = 0;
-  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit, ++k) {
-    if (!stage_next(S, chunks, segs, rec32, k, ch + nsplit, nchunks)) {
-      if (lane == 0) atomicExch(err, 1);
-      break;
-    }
-    const WorkChunk w = chunks[ch];
-    const ClassSeg sg = segs[w.cls];
-    const float* st = S.buf[k & 1];
-    const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
-    const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
-    uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
-    if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
-    if (lane == 0) {
-      nskip += w.count - __popc(m);
-      nlive += __popc(m);
-    }
-    uint32_t nm[kPPT];
-#pragma unroll
-    for (int p = 0; p < kPPT; ++p) nm[p] = 0u;
-    while (m) {
-      const int q = __ffs(m) - 1;
-      m &= m - 1;
-      float t[kPPT], e[kPPT];
-      terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
-#pragma unroll
-      for (int p = 0; p < kPPT; ++p) {
-        if (kFuse && e[p] > tau[p]) {
-          nm[p] |= 1u << q;
-          t[p] = 0.0f;
-        }
-        const f2 s = two_sum(sh[p], t[p]);
-        sh[p] = s.hi;
-        sl[p] = __fadd_rn(sl[p], s.lo);
-        sa[p] = __fadd_rn(sa[p], e[p]);
-      }
-    }
+  int k = 0;  // chunks taken by this CTA so far: selects buffer and barrier phase
+  const int64_t nitems = ntiles * nsplit;
+  for (;;) {
+    const int64_t item = next_item(work);
+    if (item >= nitems) break;
+    const int64_t wtile = item / nsplit;
+    const int split = static_cast<int>(item - wtile * nsplit);
+    const TileInfo T = tiles[wtile];
+    const ChunkRange cr = mol_chunks[T.mol];
+    const int first = cr.begin + split;
+    if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
+    float rh[3][kPPT], rl[3][kPPT];
+    load_points(phi, plo, T, lane, rh, rl);
+    float tau[kPPT];
+    f2 corr[kPPT];
     if (kFuse) {
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
-        // two terms per lane and round (independent chains); a lone last term is paired with
-        // itself and the copy discarded, so the lanes of a round run the same code
-        uint32_t mm = nm[p];
-        while (__any_sync(0xffffffffu, mm != 0u)) {
-          ++nround;
-          if (!INCA_DF_PAIRS && mm) {
-            const int q = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p],
-                                   rl[1][p], rl[2][p], tab);
-            corr[p] = df_add(corr[p], tdf);
-            ++ncorr;
-          } else if (mm) {
-            const int qa = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const bool two = mm != 0u;
-            const int qb = two ? __ffs(mm) - 1 : qa;
-            if (two) mm &= mm - 1;
-            const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], rh[0][p],
-                                    rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
-            corr[p] = df_add(corr[p], r.a);
-            if (two) corr[p] = df_add(corr[p], r.b);
-            ncorr += two ? 2 : 1;
+        const int j = lane + 32 * p;
+        tau[p] = j < T.count ? pt_tau[T.start + j] : HUGE_VALF;
+        corr[p] = {0.0f, 0.0f};
+      }
+    }
+    float box[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) box[b] = wtbox[wtile * 8 + b];
+    // quartets whose bound over the tile is at most 2^thr are left out; the one-pass form
+    // raises thr to the tile's drop threshold and sums the bounds it left out (dm)
+    const float thr = (kFuse && lt_drop) ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
+    float dm = 0.0f;
+    double acc[kPPT];
+    float sh[kPPT], sl[kPPT], sa[kPPT];
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) {
+      acc[p] = 0.0;
+      sh[p] = sl[p] = sa[p] = 0.0f;
+    }
+    __syncwarp();
+    int nfold = 0;
+    bool ok = true;
+    for (int ch = first; ch < cr.end; ch += nsplit, ++k) {
+      ok = __all_sync(0xffffffffu, stage_next(S, chunks, segs, rec32, k, ch + nsplit, cr.end));
+      if (!ok) break;
+      const WorkChunk w = chunks[ch];
+      const ClassSeg sg = segs[w.cls];
+      const float* st = S.buf[k & 1];
+      const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
+      const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
+      uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
+      if (lane == 0) {
+        nskip += w.count - __popc(m);
+        nlive += __popc(m);
+      }
+      uint32_t nm[kPPT];
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) nm[p] = 0u;
+      while (m) {
+        const int q = __ffs(m) - 1;
+        m &= m - 1;
+        float t[kPPT], e[kPPT];
+        terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) {
+          if (kFuse && e[p] > tau[p]) {
+            nm[p] |= 1u << q;
+            t[p] = 0.0f;
+          }
+          const f2 s2 = two_sum(sh[p], t[p]);
+          sh[p] = s2.hi;
+          sl[p] = __fadd_rn(sl[p], s2.lo);
+          sa[p] = __fadd_rn(sa[p], e[p]);
+        }
+      }
+      if (kFuse) {
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) {
+          // two terms per lane and round (independent chains); a lone last term is paired
+          // with itself and the copy discarded, so the lanes of a round run the same code
+          uint32_t mm = nm[p];
+          while (__any_sync(0xffffffffu, mm != 0u)) {
+            ++nround;
+            if (!INCA_DF_PAIRS && mm) {
+              const int q = __ffs(mm) - 1;
+              mm &= mm - 1;
+              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p],
+                                     rl[0][p], rl[1][p], rl[2][p], tab);
+              corr[p] = df_add(corr[p], tdf);
+              ++ncorr;
+            } else if (mm) {
+              const int qa = __ffs(mm) - 1;
+              mm &= mm - 1;
+              const bool two = mm != 0u;
+              const int qb = two ? __ffs(mm) - 1 : qa;
+              if (two) mm &= mm - 1;
+              const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], rh[0][p],
+                                      rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
+              corr[p] = df_add(corr[p], r.a);
+              if (two) corr[p] = df_add(corr[p], r.b);
+              ncorr += two ? 2 : 1;
+            }
           }
         }
       }
-    }
-    // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
-    const bool fold = ++nfold == kFold;
+      // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
+      const bool fold = ++nfold == kFold;
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) {
-      const f2 r = fast_two_sum(sh[p], sl[p]);
-      sh[p] = r.hi;
-      sl[p] = r.lo;
-      if (fold) {
-        acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
-        sh[p] = sl[p] = 0.0f;
-        if (kFuse) {
-          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-          corr[p] = {0.0f, 0.0f};
+      for (int p = 0; p < kPPT; ++p) {
+        const f2 r = fast_two_sum(sh[p], sl[p]);
+        sh[p] = r.hi;
+        sl[p] = r.lo;
+        if (fold) {
+          acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
+          sh[p] = sl[p] = 0.0f;
+          if (kFuse) {
+            acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+            corr[p] = {0.0f, 0.0f};
+          }
         }
       }
+      if (fold) nfold = 0;
+      __syncwarp();
     }
-    if (fold) nfold = 0;
-    __syncwarp();
-  }
+    if (!ok) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
-    if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-    const int64_t i = base + lane + 32 * p;
-    if (i < ngrid) {
-      part[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc[p];
-      part_abs[static_cast<int64_t>(blockIdx.y) * ngrid + i] = static_cast<double>(sa[p]);
+    for (int p = 0; p < kPPT; ++p) {
+      acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
+      if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+      const int j = lane + 32 * p;
+      if (j < T.count) {
+        part[static_cast<int64_t>(split) * ngrid + T.start + j] = acc[p];
+        part_abs[static_cast<int64_t>(split) * ngrid + T.start + j] = static_cast<double>(sa[p]);
+      }
+    }
+    if (kFuse && drop_mass) {
+      for (int o = 16; o > 0; o >>= 1) dm += __shfl_xor_sync(0xffffffffu, dm, o);
+      // the FP32 sum of the left-out bounds, raised by a margin for its own rounding
+      if (lane == 0) drop_mass[static_cast<int64_t>(split) * ntiles + wtile] = dm * 1.0001;
     }
   }
-  if (kFuse) {
-    for (int o = 16; o > 0; o >>= 1) {
-      ncorr += __shfl_xor_sync(0xffffffffu, ncorr, o);
-      dm += __shfl_xor_sync(0xffffffffu, dm, o);
-    }
-    // the FP32 sum of the left-out bounds, raised by a margin for its own rounding
-    if (lane == 0 && drop_mass) drop_mass[blockIdx.y * static_cast<int64_t>(gridDim.x) + wtile] = dm * 1.0001;
-  }
+  if (kFuse)
+    for (int o = 16; o > 0; o >>= 1) ncorr += __shfl_xor_sync(0xffffffffu, ncorr, o);
   if (lane == 0) {
     atomicAdd(&stats[2], nskip);
     if (kFuse) {
@@ -697,107 +724,123 @@ k_pass1(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __res
 
 // ---------------------------------------------------------------- pass 2 (corrections)
 __global__ void __launch_bounds__(32, 16)
-k_pass2(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __restrict__ segs,
-        const float* __restrict__ rec32, const float4* __restrict__ phi, const float4* __restrict__ plo,
-        const float* __restrict__ wtbox, const float* __restrict__ gbox, const float* __restrict__ g_lt,
-        const float* __restrict__ pt_tau, const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop,
-        const float2* __restrict__ exp_tab, int64_t ngrid, int nsplit, int stage_floats, double* __restrict__ part,
-        unsigned long long* __restrict__ stats, int* __restrict__ err) {
+k_pass2(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol_chunks,
+        const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
+        const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
+        const float* __restrict__ gbox, const float* __restrict__ g_lt, const float* __restrict__ pt_tau,
+        const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop, const float2* __restrict__ exp_tab,
+        int64_t ntiles, int nsplit, int64_t ngrid, int stage_floats, double* __restrict__ part,
+        unsigned long long* __restrict__ work, unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kExpTab + 1];
   const int lane = threadIdx.x;
-  const int64_t wtile = blockIdx.x;
-  const int64_t base = wtile * kWarpTile;
-  stage_begin(S, chunks, segs, rec32, blockIdx.y, nchunks);
   for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
-  float rh[3][kPPT], rl[3][kPPT], tau[kPPT], tau_est[kPPT];
-  load_points(phi, plo, base, lane, ngrid, rh, rl);
-#pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    const int64_t i = base + lane + 32 * p;
-    tau[p] = i < ngrid ? pt_tau[i] : HUGE_VALF;
-    tau_est[p] = (pt_tau_est && i < ngrid) ? pt_tau_est[i] : HUGE_VALF;
-  }
-  float wbox[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) wbox[k] = wtbox[wtile * 8 + k];
-  const float thr = lt_drop ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
-  double acc[kPPT];
-  f2 corr[kPPT];
-#pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    acc[p] = 0.0;
-    corr[p] = {0.0f, 0.0f};
-  }
-  __syncwarp();
+  stage_init(S);
   unsigned long long n32 = 0, ndf = 0, npts = 0;
-  int nfold = 0, k = 0;
-  for (int ch = blockIdx.y; ch < nchunks; ch += nsplit, ++k) {
-    if (!stage_next(S, chunks, segs, rec32, k, ch + nsplit, nchunks)) {
-      if (lane == 0) atomicExch(err, 1);
-      break;
-    }
-    const WorkChunk w = chunks[ch];
-    const ClassSeg sg = segs[w.cls];
-    const float* st = S.buf[k & 1];
-    const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
-    const float* Rq = st + lane * sg.stride32;
-    // pass 1's skip decision for this quartet (same box, same arithmetic, same threshold)
-    const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
-    const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
-    uint32_t msub[kPPT];
-    uint32_t any = 0;
+  int k = 0;
+  const int64_t nitems = ntiles * nsplit;
+  for (;;) {
+    const int64_t item = next_item(work);
+    if (item >= nitems) break;
+    const int64_t wtile = item / nsplit;
+    const int split = static_cast<int>(item - wtile * nsplit);
+    const TileInfo T = tiles[wtile];
+    const ChunkRange cr = mol_chunks[T.mol];
+    // a tile none of whose sub-tiles can need a correction contributes zeros
+    bool any_sub = false;
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) any_sub |= g_lt[wtile * kPPT + p] < HUGE_VALF;
+    const int first = any_sub ? cr.begin + split : cr.end;
+    if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
+    float rh[3][kPPT], rl[3][kPPT], tau[kPPT], tau_est[kPPT];
+    load_points(phi, plo, T, lane, rh, rl);
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
-      float lerr = -HUGE_VALF;
-      if (lane < w.count) log2_bound(Rq, L, gbox + (wtile * kPPT + p) * 8, &lerr);
-      msub[p] = __ballot_sync(0xffffffffu, lane < w.count && lerr > g_lt[wtile * kPPT + p]);
-      any |= msub[p];
+      const int j = lane + 32 * p;
+      tau[p] = j < T.count ? pt_tau[T.start + j] : HUGE_VALF;
+      tau_est[p] = (pt_tau_est && j < T.count) ? pt_tau_est[T.start + j] : HUGE_VALF;
     }
-    if (lane == 0) {
-      ndf += __popc(any);
-      n32 += __popc(live & ~any);
-    }
+    float wbox[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) wbox[b] = wtbox[wtile * 8 + b];
+    const float thr = lt_drop ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
+    double acc[kPPT];
+    f2 corr[kPPT];
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
-      uint32_t m = msub[p];
-      const float ph[3][1] = {{rh[0][p]}, {rh[1][p]}, {rh[2][p]}};
-      const float pl[3][1] = {{rl[0][p]}, {rl[1][p]}, {rl[2][p]}};
-      while (m) {
-        const int q = __ffs(m) - 1;
-        m &= m - 1;
-        const float* R = st + q * sg.stride32;
-        float t32[1], e32[1];
-        term32_one(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], t32, e32);
-        // with pt_tau_est: the one-pass kernel already corrected the live terms above tau_est
-        const bool live_q = (live >> q) & 1u;
-        const bool need = e32[0] > tau[p] && !(live_q && e32[0] > tau_est[p]);
-        if (__any_sync(0xffffffffu, need)) {
-          if (lane == 0) ++npts;
-          if (need) {
-            f2 tdf = term_df(R, L[0], L[1], L[2], ph[0][0], ph[1][0], ph[2][0], pl[0][0], pl[1][0], pl[2][0], tab);
-            if (live_q) tdf = df_add(tdf, f2{-t32[0], 0.0f});
-            corr[p] = df_add(corr[p], tdf);
+      acc[p] = 0.0;
+      corr[p] = {0.0f, 0.0f};
+    }
+    __syncwarp();
+    int nfold = 0;
+    bool ok = true;
+    for (int ch = first; ch < cr.end; ch += nsplit, ++k) {
+      ok = __all_sync(0xffffffffu, stage_next(S, chunks, segs, rec32, k, ch + nsplit, cr.end));
+      if (!ok) break;
+      const WorkChunk w = chunks[ch];
+      const ClassSeg sg = segs[w.cls];
+      const float* st = S.buf[k & 1];
+      const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
+      const float* Rq = st + lane * sg.stride32;
+      // the skip decision of the pass over all terms (same box, arithmetic and threshold)
+      const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
+      const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      uint32_t msub[kPPT];
+      uint32_t any = 0;
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) {
+        float lerr = -HUGE_VALF;
+        if (lane < w.count) log2_bound(Rq, L, gbox + (wtile * kPPT + p) * 8, &lerr);
+        msub[p] = __ballot_sync(0xffffffffu, lane < w.count && lerr > g_lt[wtile * kPPT + p]);
+        any |= msub[p];
+      }
+      if (lane == 0) {
+        ndf += __popc(any);
+        n32 += __popc(live & ~any);
+      }
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) {
+        uint32_t m = msub[p];
+        while (m) {
+          const int q = __ffs(m) - 1;
+          m &= m - 1;
+          const float* R = st + q * sg.stride32;
+          float t32 = 0.0f, e32 = 0.0f;
+          term32_one(R, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], &t32, &e32);
+          // with pt_tau_est: the one-pass kernel already corrected the live terms above it
+          const bool live_q = (live >> q) & 1u;
+          const bool need = e32 > tau[p] && !(live_q && e32 > tau_est[p]);
+          if (__any_sync(0xffffffffu, need)) {
+            if (lane == 0) ++npts;
+            if (need) {
+              f2 tdf = term_df(R, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
+              if (live_q) tdf = df_add(tdf, f2{-t32, 0.0f});
+              corr[p] = df_add(corr[p], tdf);
+            }
           }
         }
       }
-    }
-    if (++nfold == kFold) {
-      nfold = 0;
+      if (++nfold == kFold) {
+        nfold = 0;
 #pragma unroll
-      for (int p = 0; p < kPPT; ++p) {
-        acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-        corr[p] = {0.0f, 0.0f};
+        for (int p = 0; p < kPPT; ++p) {
+          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+          corr[p] = {0.0f, 0.0f};
+        }
       }
+      __syncwarp();
     }
-    __syncwarp();
-  }
+    if (!ok) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
 #pragma unroll
-  for (int p = 0; p < kPPT; ++p) {
-    acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-    const int64_t i = base + lane + 32 * p;
-    if (i < ngrid) part[static_cast<int64_t>(blockIdx.y) * ngrid + i] = acc[p];
+    for (int p = 0; p < kPPT; ++p) {
+      acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+      const int j = lane + 32 * p;
+      if (j < T.count) part[static_cast<int64_t>(split) * ngrid + T.start + j] = acc[p];
+    }
   }
   if (lane == 0) {
     atomicAdd(&stats[0], n32);
@@ -859,17 +902,18 @@ __global__ void k_gather_points(int64_t n, const int64_t* __restrict__ perm, con
 
 // Bounding boxes (FP32, rounded outwards) of each 128-point tile and its four 32-point
 // sub-tiles (points lane + 32 p). One warp per tile.
-__global__ void k_boxes(int64_t n, int64_t nwt, const float4* __restrict__ phi, const float4* __restrict__ plo,
-                        float* wbox, float* gbox) {
+__global__ void k_boxes(const TileInfo* __restrict__ tiles, int64_t nwt, const float4* __restrict__ phi,
+                        const float4* __restrict__ plo, float* wbox, float* gbox) {
   const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (wt >= nwt) return;
   const int lane = threadIdx.x & 31;
+  const TileInfo T = tiles[wt];
   float tlo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF}, thi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
   for (int p = 0; p < kPPT; ++p) {
-    const int64_t i = wt * kWarpTile + lane + 32 * p;
+    const int j = lane + 32 * p;
     float lo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF}, hi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
-    if (i < n) {
-      const float4 h = phi[i], l = plo[i];
+    if (j < T.count) {
+      const float4 h = phi[T.start + j], l = plo[T.start + j];
       const float x[3] = {h.x + l.x, h.y + l.y, h.z + l.z};
       for (int d = 0; d < 3; ++d) lo[d] = hi[d] = x[d];
     }
@@ -899,17 +943,20 @@ __global__ void k_boxes(int64_t n, int64_t nwt, const float4* __restrict__ phi, 
 // A term is corrected when its error bound e exceeds tau_g / 1.01 (the stored value).
 // mode 0: tau = T_seg / w_g; mode 1 (max-norm): tau = T / E_g; mode 2: per point;
 // mode 3: tau = T (uniform).
-__global__ void k_thresholds(int64_t n, int64_t ngroups, int mode, const int64_t* __restrict__ perm,
-                             const int* __restrict__ seg_of, const double* __restrict__ segT,
-                             const double* __restrict__ w, const double* __restrict__ I,
-                             const double* __restrict__ M, double eps, double tscale, float* g_lt, float* pt_tau) {
+__global__ void k_thresholds(const TileInfo* __restrict__ tiles, int64_t ngroups, int mode,
+                             const int64_t* __restrict__ perm, const int* __restrict__ seg_of,
+                             const double* __restrict__ segT, const double* __restrict__ w,
+                             const double* __restrict__ I, const double* __restrict__ M, double eps, double tscale,
+                             float* g_lt, float* pt_tau) {
   const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (grp >= ngroups) return;
   const int lane = threadIdx.x & 31;
-  // group grp = tile grp / kPPT, sub-tile grp % kPPT: points tile*128 + lane + 32*sub
-  const int64_t i = (grp / kPPT) * kWarpTile + lane + 32 * (grp % kPPT);
+  // group grp = tile grp / kPPT, sub-tile grp % kPPT: the tile's points lane + 32 * sub
+  const TileInfo T = tiles[grp / kPPT];
+  const int j = lane + 32 * static_cast<int>(grp % kPPT);
+  const int64_t i = T.start + j;
   float ts = HUGE_VALF;
-  if (i < n) {
+  if (j < T.count) {
     const int64_t g = perm[i];
     double tau = HUGE_VAL;
     if (mode == 0) {
@@ -935,14 +982,16 @@ __global__ void k_thresholds(int64_t n, int64_t ngroups, int mode, const int64_t
 
 // Sub-tiles where the exact threshold fell below the estimate used by the one-pass kernel:
 // g_lt = log2 of the smallest exact threshold among those points (else +inf); counts them.
-__global__ void k_band(int64_t n, int64_t ngroups, const float* __restrict__ pt_tau,
+__global__ void k_band(const TileInfo* __restrict__ tiles, int64_t ngroups, const float* __restrict__ pt_tau,
                        const float* __restrict__ pt_tau_est, float* g_lt, unsigned long long* nband) {
   const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (grp >= ngroups) return;
   const int lane = threadIdx.x & 31;
-  const int64_t i = (grp / kPPT) * kWarpTile + lane + 32 * (grp % kPPT);
+  const TileInfo T = tiles[grp / kPPT];
+  const int j = lane + 32 * static_cast<int>(grp % kPPT);
+  const int64_t i = T.start + j;
   float t = HUGE_VALF;
-  if (i < n && pt_tau[i] < pt_tau_est[i]) t = pt_tau[i];
+  if (j < T.count && pt_tau[i] < pt_tau_est[i]) t = pt_tau[i];
   for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
   if (lane == 0) {
     g_lt[grp] = t >= HUGE_VALF ? HUGE_VALF : (t > 0.0f ? log2f(t) : -HUGE_VALF);
@@ -1025,24 +1074,29 @@ __global__ void k_seg_sums(int nseg, const int64_t* __restrict__ off, const doub
 }
 
 // log2 of the smallest per-point value of each 128-point tile (one warp per tile).
-__global__ void k_tile_min_log2(int64_t n, int64_t nwt, const float* __restrict__ pt, float* lt) {
+__global__ void k_tile_min_log2(const TileInfo* __restrict__ tiles, int64_t nwt, const float* __restrict__ pt,
+                                float* lt) {
   const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
   if (wt >= nwt) return;
   const int lane = threadIdx.x & 31;
+  const TileInfo T = tiles[wt];
   float t = HUGE_VALF;
   for (int p = 0; p < kPPT; ++p) {
-    const int64_t i = wt * kWarpTile + lane + 32 * p;
-    if (i < n) t = fminf(t, pt[i]);
+    const int j = lane + 32 * p;
+    if (j < T.count) t = fminf(t, pt[T.start + j]);
   }
   for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
   if (lane == 0) lt[wt] = t >= HUGE_VALF ? HUGE_VALF : (t > 0.0f ? log2f(t) : -HUGE_VALF);
 }
 
 // Per-tile values spread to the tile's points, in grid order.
-__global__ void k_tile_to_points(int64_t n, const int64_t* __restrict__ perm, const double* __restrict__ vt,
-                                 double* out) {
-  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (i < n) out[perm[i]] = vt[i / kWarpTile];
+__global__ void k_tile_to_points(const TileInfo* __restrict__ tiles, int64_t nwt, const int64_t* __restrict__ perm,
+                                 const double* __restrict__ vt, double* out) {
+  const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
+  if (wt >= nwt) return;
+  const int lane = threadIdx.x & 31;
+  const TileInfo T = tiles[wt];
+  for (int j = lane; j < T.count; j += 32) out[perm[T.start + j]] = vt[wt];
 }
 
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
@@ -1050,11 +1104,17 @@ inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
 // permutation (sorted position -> grid index) and the tile / sub-tile boxes.
 int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, DevBuf<float4>& phi,
-                DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, int64_t* n_out) {
+                DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, DevBuf<TileInfo>& tiles,
+                int64_t* n_out, int64_t* ntiles_out) {
   const int64_t n = (c->ngrid + stride - 1) / stride;
   const int64_t nwt = (n + kWarpTile - 1) / kWarpTile;
-  if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT))
+  if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT) ||
+      tiles.reserve(std::max<int64_t>(nwt, 1)))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
+  std::vector<TileInfo> ht(nwt);
+  for (int64_t t = 0; t < nwt; ++t)
+    ht[t] = TileInfo{t * kWarpTile, static_cast<int>(std::min<int64_t>(kWarpTile, n - t * kWarpTile)), 0};
+  if (nwt) INCA_CUDA(c, cudaMemcpy(tiles.p, ht.data(), sizeof(TileInfo) * nwt, cudaMemcpyHostToDevice));
   DevBuf<uint64_t> k1, k2;
   DevBuf<int64_t> i1;
   DevBuf<unsigned char> tmp;
@@ -1071,13 +1131,14 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
   if (!e) e = cub::DeviceRadixSort::SortPairs(tmp.p, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
   if (!e) {
     INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, phi.p, plo.p);
-    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, n, nwt, phi.p, plo.p, boxes.p,
+    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p,
                 boxes.p + 8 * nwt);
     e = cudaStreamSynchronize(c->stream);
   }
   rel();
   if (e) return cuda_error(c, e, "sorted grid");
   *n_out = n;
+  *ntiles_out = nwt;
   return INCA_OK;
 }
 
@@ -1102,13 +1163,14 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
   const double inv = 2097151.0 / ext;
   int64_t nn = 0;
   if (!main_ok) {
-    const int st = sort_points(c, 1, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, &nn);
+    const int st = sort_points(c, 1, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
+                               &c->ntiles);
     if (st) return st;
     c->mix_version = c->grid_version;
   }
   if (!sample_ok) {
     const int st = sort_points(c, kSampleStride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
-                               &c->nsample);
+                               c->d_tiles_s, &c->nsample, &c->ntiles_s);
     if (st) return st;
     c->sample_version = c->grid_version;
   }
@@ -1147,6 +1209,21 @@ std::vector<float2> exp2_table() {
   return t;
 }
 
+// Quartet splits per tile: enough (tile, split) work items for kItemsPerCta items per resident
+// CTA, so that the persistent CTAs finish together (an item is small next to the whole).
+int item_splits(int64_t ntiles, int64_t nchunks, int num_sms) {
+  const int64_t target = static_cast<int64_t>(num_sms) * INCA_PASS_CTAS_PER_SM * kItemsPerCta;
+  int64_t s = (target + std::max<int64_t>(ntiles, 1) - 1) / std::max<int64_t>(ntiles, 1);
+  s = std::max<int64_t>(1, std::min<int64_t>(s, std::max<int64_t>(nchunks, 1)));
+  return static_cast<int>(std::min<int64_t>(s, 4096));
+}
+
+// Resident CTAs of a persistent pass launch (one-warp CTAs, INCA_PASS_CTAS_PER_SM per SM).
+unsigned persistent_ctas(int64_t nitems, int num_sms) {
+  return static_cast<unsigned>(
+      std::max<int64_t>(1, std::min<int64_t>(nitems, static_cast<int64_t>(num_sms) * INCA_PASS_CTAS_PER_SM)));
+}
+
 }  // namespace
 
 int eval_mixed(inca_ctx* c, double eps) {
@@ -1165,11 +1242,13 @@ int eval_mixed(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaEventRecord(ev.e[0], c->stream));
   int st = prepare_sorted_grid(c, fused);
   if (st) return st;
-  const int64_t nwt = (ngrid + kWarpTile - 1) / kWarpTile;
+  const int64_t nwt = c->ntiles;
   const int64_t ngroups = nwt * kPPT;
-  const int nsplit = choose_splits(nwt, nchunks, c->num_sms, INCA_PASS_CTAS_PER_SM);
+  const int nsplit = item_splits(nwt, nchunks, c->num_sms);
+  const unsigned nctas = persistent_ctas(nwt * nsplit, c->num_sms);
   const float* wbox = c->d_wtbox.p;
   const float* gbox = c->d_wtbox.p + 8 * nwt;
+  const TileInfo* tiles = c->d_tiles.p;
 
   // outputs and their segments: radial grid (one integral), scan grid (one I(s) per shell),
   // cube (max-norm), explicit points (each point)
@@ -1193,7 +1272,8 @@ int eval_mixed(inca_ctx* c, double eps) {
   // thresholds, left-out bound mass per tile, statistics, the exp table, segment sums
   double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT, *dmass, *Dt, *Dpt;
   float *glt, *ptau, *ptau_est, *ptheta, *ltdrop;
-  unsigned long long *stats, *dmax;
+  unsigned long long *stats, *dmax, *work;
+  ChunkRange* mchunks;
   int* errw;
   int64_t* doff;
   float2* tab;
@@ -1214,6 +1294,8 @@ int eval_mixed(inca_ctx* c, double eps) {
     Dt = cv.take<double>(fused ? nwt : 1);
     Dpt = cv.take<double>(fused ? ngrid : 1);
     stats = cv.take<unsigned long long>(16);
+    work = cv.take<unsigned long long>(4);
+    mchunks = cv.take<ChunkRange>(1);
     dmax = cv.take<unsigned long long>(2);
     errw = cv.take<int>(4);
     tab = cv.take<float2>(kExpTab + 1);
@@ -1243,6 +1325,9 @@ int eval_mixed(inca_ctx* c, double eps) {
   const std::vector<float2> htab = exp2_table();
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), c->stream));
+  const ChunkRange all_chunks{0, nchunks};
+  INCA_CUDA(c, cudaMemcpyAsync(mchunks, &all_chunks, sizeof(ChunkRange), cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(errw, 0, 4 * sizeof(int), c->stream));
   if (!off.empty())
     INCA_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
@@ -1291,8 +1376,8 @@ int eval_mixed(inca_ctx* c, double eps) {
       if (end != env && v >= 0.0 && std::isfinite(v)) safety = v;
     }
     const int64_t ns = c->nsample;
-    const int64_t nwt_s = (ns + kWarpTile - 1) / kWarpTile;
-    const int nsplit_s = choose_splits(nwt_s, nchunks, c->num_sms, INCA_PASS_CTAS_PER_SM);
+    const int64_t nwt_s = c->ntiles_s;
+    const int nsplit_s = item_splits(nwt_s, nchunks, c->num_sms);
     double *q1, *qabs, *Iss, *Mss, *Ios, *Mos, *ws;
     auto layout_s = [&](Carve& cs) {
       q1 = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);
@@ -1308,10 +1393,9 @@ int eval_mixed(inca_ctx* c, double eps) {
     if (c->d_scratch_s.reserve(dry_s.off + 256)) return set_error(c, INCA_E_NOMEM, "sample scratch");
     Carve cs{c->d_scratch_s.p};
     layout_s(cs);
-    dim3 grid_s(static_cast<unsigned>(nwt_s), static_cast<unsigned>(nsplit_s));
-    INCA_LAUNCH(c, k_pass1<false>, grid_s, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
-                c->d_phi_s.p, c->d_plo_s.p, c->d_wtbox_s.p, ns, nsplit_s, stage_floats, nullptr, nullptr, nullptr, q1,
-                qabs, nullptr, stats + 8, errw);
+    INCA_LAUNCH(c, k_pass1<false>, persistent_ctas(nwt_s * nsplit_s, c->num_sms), 32, dsmem, c->d_chunks.p, mchunks,
+                c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, nwt_s,
+                nsplit_s, ns, stage_floats, nullptr, nullptr, nullptr, q1, qabs, nullptr, work + 3, stats + 8, errw);
     INCA_CUDA(c, cudaGetLastError());
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, q1, nullptr, Iss);
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, qabs, nullptr, Mss);
@@ -1343,33 +1427,32 @@ int eval_mixed(inca_ctx* c, double eps) {
       segTheta[0] = 0.5 * drop_frac * eps * imax / nq;
     }
     INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-    INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
+    INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
                 nullptr, eps, tau_scale, nullptr, ptau_est);
     use_drop = drop_frac > 0.0;
     if (use_drop) {
       // (pageable host copies are staged before the call returns; the stream orders the rest)
       INCA_CUDA(c, cudaMemcpyAsync(dT, segTheta.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-      INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
+      INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
                   nullptr, eps, tau_scale, nullptr, ptheta);
-      INCA_LAUNCH(c, k_tile_min_log2, tblk, 256, 0, ngrid, nwt, ptheta, ltdrop);
+      INCA_LAUNCH(c, k_tile_min_log2, tblk, 256, 0, tiles, nwt, ptheta, ltdrop);
     }
     INCA_CUDA(c, cudaGetLastError());
   }
 
-  dim3 grid(static_cast<unsigned>(nwt), static_cast<unsigned>(nsplit));
   bool run_pass2 = true;
   for (int attempt = 0;; ++attempt) {
     // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
     // terms below the drop thresholds left out)
     INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
     if (fused)
-      INCA_LAUNCH(c, k_pass1<true>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                  c->d_plo.p, wbox, ngrid, nsplit, stage_floats, ptau_est, tab, use_drop ? ltdrop : nullptr, p1, pabs,
-                  dmass, stats, errw);
+      INCA_LAUNCH(c, k_pass1<true>, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+                  c->d_plo.p, tiles, wbox, nwt, nsplit, ngrid, stage_floats, ptau_est, tab, use_drop ? ltdrop : nullptr,
+                  p1, pabs, dmass, work, stats, errw);
     else
-      INCA_LAUNCH(c, k_pass1<false>, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p,
-                  c->d_phi.p, c->d_plo.p, wbox, ngrid, nsplit, stage_floats, nullptr, nullptr, nullptr, p1, pabs,
-                  nullptr, stats, errw);
+      INCA_LAUNCH(c, k_pass1<false>, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p,
+                  c->d_phi.p, c->d_plo.p, tiles, wbox, nwt, nsplit, ngrid, stage_floats, nullptr, nullptr, nullptr, p1,
+                  pabs, nullptr, work, stats, errw);
     INCA_CUDA(c, cudaGetLastError());
     INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
     INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
@@ -1377,7 +1460,7 @@ int eval_mixed(inca_ctx* c, double eps) {
     INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
     if (use_drop) {
       INCA_LAUNCH(c, k_sum_splits, nblk(nwt), 256, 0, nwt, nsplit, dmass, nullptr, Dt);
-      INCA_LAUNCH(c, k_tile_to_points, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Dt, Dpt);
+      INCA_LAUNCH(c, k_tile_to_points, tblk, 256, 0, tiles, nwt, c->d_perm.p, Dt, Dpt);
     }
 
     // ---- exact thresholds of the outputs
@@ -1412,16 +1495,17 @@ int eval_mixed(inca_ctx* c, double eps) {
     if (retry && attempt == 0) {  // too much was left out: once more without leaving terms out
       use_drop = false;
       INCA_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), c->stream));
+      INCA_CUDA(c, cudaMemsetAsync(work, 0, sizeof(unsigned long long), c->stream));
       continue;
     }
     break;
   }
   INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-  INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, ngrid, ngroups, mode, c->d_perm.p, seg_of, dT, c->d_w.p, Is, Ms, eps,
+  INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, mode, c->d_perm.p, seg_of, dT, c->d_w.p, Is, Ms, eps,
               tau_scale, fused ? nullptr : glt, ptau);
   INCA_CUDA(c, cudaGetLastError());
   if (fused) {
-    INCA_LAUNCH(c, k_band, gblk, 256, 0, ngrid, ngroups, ptau, ptau_est, glt, stats + 12);
+    INCA_LAUNCH(c, k_band, gblk, 256, 0, tiles, ngroups, ptau, ptau_est, glt, stats + 12);
     unsigned long long nband = 0;
     INCA_CUDA(c, cudaMemcpyAsync(&nband, stats + 12, sizeof(nband), cudaMemcpyDeviceToHost, c->stream));
     INCA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1429,9 +1513,9 @@ int eval_mixed(inca_ctx* c, double eps) {
   }
   INCA_CUDA(c, cudaEventRecord(ev.e[3], c->stream));
   if (run_pass2) {
-    INCA_LAUNCH(c, k_pass2, grid, 32, dsmem, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                c->d_plo.p, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, use_drop ? ltdrop : nullptr, tab, ngrid,
-                nsplit, stage_floats, p2, stats + 4, errw);
+    INCA_LAUNCH(c, k_pass2, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+                c->d_plo.p, tiles, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, use_drop ? ltdrop : nullptr, tab,
+                nwt, nsplit, ngrid, stage_floats, p2, work + 1, stats + 4, errw);
     INCA_CUDA(c, cudaGetLastError());
   }
   INCA_CUDA(c, cudaEventRecord(ev.e[4], c->stream));
