@@ -58,6 +58,11 @@ SIGNATURES = {
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
     "inca_fp32_fma_peak": (ctypes.c_int, [VP, DP]),
+    "inca_batch_clear": (ctypes.c_int, [VP]),
+    "inca_batch_add_closed_shell": (ctypes.c_int, [VP, ctypes.c_int32, DP, IP, DP, DP, DP, DP, ctypes.c_int,
+                                                   ctypes.c_int32, DP, DP, DP, IP, ctypes.c_int, IP]),
+    "inca_batch_prepare": (ctypes.c_int, [VP, ctypes.c_double, ctypes.POINTER(Counts), I64P]),
+    "inca_batch_eval": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_double, DP]),
     "inca_eval_records_noalloc": (ctypes.c_int, [ctypes.c_int64, VP, VP, VP, VP, VP, ctypes.c_int64, VP, VP, VP]),
 }
 
@@ -161,6 +166,47 @@ class Context:
         n = ctypes.c_int64()
         self._check(self.lib.inca_gen_closed_shell_dm2(self.h, _d(D), int(unique), ctypes.byref(n)))
         return n.value
+
+    # ---- batches of molecules (radial-scan I(s) for each, evaluated together)
+    def batch_clear(self):
+        self._check(self.lib.inca_batch_clear(self.h))
+        self.batch_nradi = []
+
+    def batch_add_closed_shell(self, alpha, tmn, xyz, D, start, end, step, nang, unique=False, nosym=False):
+        alpha = f64(alpha)
+        n = len(alpha)
+        tmn_cm = i32(np.asarray(tmn, dtype=np.int32).reshape(n, 3).T.reshape(-1))
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(n, 3)
+        xs, ys, zs = f64(xyz[:, 0]), f64(xyz[:, 1]), f64(xyz[:, 2])
+        Dc = f64(np.asarray(D, dtype=np.float64).T.reshape(-1))
+        start, end, step, nang = f64(start), f64(end), f64(step), i32(nang)
+        nr = ctypes.c_int32()
+        self._check(self.lib.inca_batch_add_closed_shell(self.h, n, _d(alpha), _i(tmn_cm), _d(xs), _d(ys), _d(zs),
+                                                         _d(Dc), int(unique), len(start), _d(start), _d(end),
+                                                         _d(step), _i(nang), int(nosym), ctypes.byref(nr)))
+        if not hasattr(self, "batch_nradi"):
+            self.batch_nradi = []
+        self.batch_nradi.append(nr.value)
+        return nr.value
+
+    def batch_prepare(self, thresh):
+        c = Counts()
+        ng = ctypes.c_int64()
+        self._check(self.lib.inca_batch_prepare(self.h, thresh, ctypes.byref(c), ctypes.byref(ng)))
+        self.counts = (c.read, c.after_screen1, c.after_screen2)
+        self.nradi = int(sum(self.batch_nradi))
+        self.ngrid = ng.value
+        return self.counts
+
+    def batch_eval(self, mode=INCA_MIXED, tol=1e-8):
+        """I(s) of every molecule of the batch, as a list of arrays (one per molecule)."""
+        out = np.zeros(int(sum(self.batch_nradi)))
+        self._check(self.lib.inca_batch_eval(self.h, mode, tol, _d(out)))
+        parts, k = [], 0
+        for nr in self.batch_nradi:
+            parts.append(out[k:k + nr])
+            k += nr
+        return parts
 
     def prepare(self, thresh, normalize=True):
         c = Counts()

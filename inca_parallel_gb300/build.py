@@ -30,6 +30,7 @@ UNITS = {
     "grid_build.cu": ["-fmad=false"],
     "noalloc_eval.cu": [],
     "peak_probe.cu": [],
+    "batch.cu": [],
     "host_tables.cpp": [],
 }
 DRIVER_SRC = os.path.join(CSRC, "driver", "inca_main.cpp")

@@ -31,6 +31,23 @@ static long long dfact(int a) {
   return r;
 }
 
+PrimD make_prim(double alpha, const int t[3], double x, double y, double z, int nprim_mol, int mol) {
+  PrimD q;
+  q.alpha = alpha;
+  q.x = x;
+  q.y = y;
+  q.z = z;
+  for (int d = 0; d < 3; ++d) q.t[d] = t[d];
+  q.mol = mol;
+  q.lim_scale = 1.0 / (double(nprim_mol) * (double(nprim_mol) + 1.0) * 0.5);
+  // normprim (src/mod_intracule.f90:145-152)
+  const double pi = 4.0 * std::atan(1.0);
+  const int L = t[0] + t[1] + t[2];
+  const double df = double(dfact(2 * t[0] - 1) * dfact(2 * t[1] - 1) * dfact(2 * t[2] - 1));
+  q.norm = std::pow(2.0 * alpha / pi, 0.75) * std::sqrt(std::pow(4.0 * alpha, double(L)) * (1.0 / df));
+  return q;
+}
+
 }  // namespace inca
 
 using namespace inca;
@@ -119,29 +136,21 @@ int inca_set_primitives(inca_ctx* c, int32_t nprim, const double* alpha, const i
   c->h_y.assign(yn, yn + nprim);
   c->h_z.assign(zn, zn + nprim);
   c->h_tmn.assign(3 * static_cast<size_t>(nprim), 0);
-  const double pi = 4.0 * std::atan(1.0);
   for (int p = 0; p < nprim; ++p) {
     if (!(alpha[p] > 0.0)) return set_error(c, INCA_E_ARG, "inca_set_primitives: exponent <= 0 or NaN at primitive " + std::to_string(p + 1));
-    PrimD& q = h[p];
-    q.alpha = alpha[p];
-    q.x = xn[p];
-    q.y = yn[p];
-    q.z = zn[p];
+    int t[3];
     for (int d = 0; d < 3; ++d) {
-      q.t[d] = tmn[p + static_cast<size_t>(nprim) * d];  // TMN(nprim,3), column-major
-      if (q.t[d] < 0) return set_error(c, INCA_E_ARG, "inca_set_primitives: negative Cartesian power");
-      c->h_tmn[3 * p + d] = q.t[d];
+      t[d] = tmn[p + static_cast<size_t>(nprim) * d];  // TMN(nprim,3), column-major
+      if (t[d] < 0) return set_error(c, INCA_E_ARG, "inca_set_primitives: negative Cartesian power");
+      c->h_tmn[3 * p + d] = t[d];
     }
-    q.pad = 0;
-    // normprim (src/mod_intracule.f90:145-152)
-    const int L = q.t[0] + q.t[1] + q.t[2];
-    const double df = double(dfact(2 * q.t[0] - 1) * dfact(2 * q.t[1] - 1) * dfact(2 * q.t[2] - 1));
-    q.norm = std::pow(2.0 * q.alpha / pi, 0.75) * std::sqrt(std::pow(4.0 * q.alpha, double(L)) * (1.0 / df));
+    h[p] = make_prim(alpha[p], t, xn[p], yn[p], zn[p], nprim, 0);
   }
   if (c->d_prims.reserve(nprim)) return set_error(c, INCA_E_NOMEM, "primitives");
   INCA_CUDA(c, cudaMemcpyAsync(c->d_prims.p, h.data(), sizeof(PrimD) * nprim, cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->nprim = nprim;
+  c->batch_molecules = 0;
   c->prepared = false;
   c->evaluated = false;
   return INCA_OK;

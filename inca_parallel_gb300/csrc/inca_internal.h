@@ -44,10 +44,12 @@ struct DevBuf {
 };
 
 // One primitive as the device kernels read it.
+// lim_scale = 1 / (nprim (nprim + 1) / 2) of the primitive's molecule (the screening limit is
+// thresh * lim_scale, src/mod_intracule.f90:163); mol: molecule index within a batch (else 0).
 struct PrimD {
-  double alpha, x, y, z, norm;
+  double alpha, x, y, z, norm, lim_scale;
   int t[3];
-  int pad;
+  int mol;
 };
 
 // Angular class of survivors: all records of a class share (Lx, Ly, Lz) and a stride.
@@ -59,7 +61,7 @@ struct ClassSeg {
   int64_t off64;    // offset of the segment in the FP64 record array (doubles)
   int64_t off32;    // offset of the segment in the FP32 record array (floats)
   int stride32;     // floats per FP32 record (multiple of 4)
-  int pad;
+  int mol;          // molecule of the segment (0 unless batched)
 };
 
 // A chunk of <= kChunk records of one class: the unit of work of the evaluation kernels.
@@ -80,6 +82,18 @@ struct TileInfo {
 // The chunk range [begin, end) of one molecule.
 struct ChunkRange {
   int begin, end;
+};
+
+// One molecule of a batch, as added (host copies until the batch is prepared).
+struct BatchMol {
+  int nprim = 0;
+  std::vector<double> alpha, x, y, z, D;
+  std::vector<int> tmn;  // row-major nprim x 3
+  int unique = 0;
+  std::vector<double> start, end, step;
+  std::vector<int> nang;
+  int nosym = 0;
+  int nradi = 0;
 };
 
 enum GridKind { GRID_NONE = 0, GRID_RADIAL = 1, GRID_SCAN = 2, GRID_CUBE = 3, GRID_POINTS = 4 };
@@ -121,6 +135,14 @@ struct inca_ctx {
   inca::DevBuf<float> d_rec32;      // FP32 records (mixed form), class segments
   inca::DevBuf<int64_t> d_surv_src; // input index of each class-sorted survivor
   int max_L = 0;
+  int batch_molecules = 0;                   // molecules of the current batch (0: not batched)
+  std::vector<inca::BatchMol> batch;         // molecules added since inca_batch_clear
+  std::vector<int64_t> h_mol_off;            // first grid point of each molecule (+ total)
+  std::vector<int> h_mol_shell_off;          // first shell of each molecule (+ total)
+  inca::DevBuf<int> d_pmol;                  // molecule of each grid point (batch grids)
+  int64_t batch_grid_version = -1;
+  std::vector<inca::ChunkRange> mol_chunks;  // chunk range of each molecule (one entry unless batched)
+  std::vector<int64_t> mol_surv;             // survivors of each molecule
 
   // grid
   int grid_kind = inca::GRID_NONE;
@@ -168,11 +190,14 @@ struct inca_ctx {
 namespace inca {
 
 int set_error(inca_ctx* c, int code, const std::string& msg);
+PrimD make_prim(double alpha, const int t[3], double x, double y, double z, int nprim_mol, int mol);
 int cuda_error(inca_ctx* c, cudaError_t e, const char* what);
 
 // quartet_prep.cu
 int prepare_device(inca_ctx* c, double thresh, int normalize);
 int gen_closed_shell_device(inca_ctx* c, const double* D, int unique, int64_t* nrec);
+int64_t closed_shell_records(int n, int unique);
+int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int base, int64_t at);
 
 // intracule_eval.cu
 int eval_device(inca_ctx* c, int mode, double tol);

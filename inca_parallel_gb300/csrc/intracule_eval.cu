@@ -101,6 +101,8 @@ int choose_splits(int64_t tiles, int64_t nchunks, int num_sms, int ctas_per_sm) 
 int eval_device(inca_ctx* c, int mode, double tol) {
   if (!c->prepared) return set_error(c, INCA_E_STATE, "inca_eval: call inca_prepare first");
   if (c->grid_kind == GRID_NONE || c->ngrid <= 0) return set_error(c, INCA_E_STATE, "inca_eval: no grid");
+  if (c->batch_molecules > 0 && c->batch_grid_version != c->grid_version)
+    return set_error(c, INCA_E_STATE, "inca_eval: the batch's grid was replaced; prepare the batch again");
   if (c->d_ivec.reserve(c->ngrid)) return set_error(c, INCA_E_NOMEM, "ivec");
   c->t_total_ms = c->t_kernel_ms = c->t_pass2_ms = 0;
   c->t_kernel_launches = c->t_launches = 0;
@@ -123,18 +125,32 @@ int eval_device(inca_ctx* c, int mode, double tol) {
     c->evaluated = true;
     return INCA_OK;
   }
-  const int64_t tiles = (ngrid + kTile64 - 1) / kTile64;
-  const int nsplit = choose_splits(tiles, nchunks, c->num_sms, 4);
-  if (c->d_partial.reserve(static_cast<size_t>(nsplit) * ngrid)) return set_error(c, INCA_E_NOMEM, "partials");
+  // one launch pair per molecule of a batch (each molecule's points against its own chunks)
+  const int nmol = c->batch_molecules > 0 ? c->batch_molecules : 1;
   INCA_CUDA(c, cudaEventRecord(e0, c->stream));
-  dim3 grid(static_cast<unsigned>(tiles), static_cast<unsigned>(nsplit));
-  INCA_LAUNCH(c, k_eval_fp64, grid, kThreads64, 0, c->d_chunks.p, nchunks, c->d_classes.p, c->d_rec64.p, c->d_px.p,
-                                                  c->d_py.p, c->d_pz.p, ngrid, nsplit, c->d_partial.p);
-  INCA_CUDA(c, cudaGetLastError());
+  int launches = 0;
+  for (int m = 0; m < nmol; ++m) {
+    const int64_t p0 = c->batch_molecules > 0 ? c->h_mol_off[m] : 0;
+    const int64_t np = c->batch_molecules > 0 ? c->h_mol_off[m + 1] - p0 : ngrid;
+    const int cb = c->mol_chunks[m].begin, nch = c->mol_chunks[m].end - c->mol_chunks[m].begin;
+    if (np == 0) continue;
+    if (nch <= 0) {
+      INCA_CUDA(c, cudaMemsetAsync(c->d_ivec.p + p0, 0, sizeof(double) * np, c->stream));
+      continue;
+    }
+    const int64_t tiles = (np + kTile64 - 1) / kTile64;
+    const int nsplit = choose_splits(tiles, nch, c->num_sms, 4);
+    if (c->d_partial.reserve(static_cast<size_t>(nsplit) * np)) return set_error(c, INCA_E_NOMEM, "partials");
+    dim3 grid(static_cast<unsigned>(tiles), static_cast<unsigned>(nsplit));
+    INCA_LAUNCH(c, k_eval_fp64, grid, kThreads64, 0, c->d_chunks.p + cb, nch, c->d_classes.p, c->d_rec64.p,
+                c->d_px.p + p0, c->d_py.p + p0, c->d_pz.p + p0, np, nsplit, c->d_partial.p);
+    INCA_CUDA(c, cudaGetLastError());
+    INCA_LAUNCH(c, k_reduce_splits, static_cast<unsigned>((np + 255) / 256), 256, 0, c->d_partial.p, nsplit, np,
+                c->d_ivec.p + p0);
+    INCA_CUDA(c, cudaGetLastError());
+    launches += 2;
+  }
   INCA_CUDA(c, cudaEventRecord(e1, c->stream));
-  INCA_LAUNCH(c, k_reduce_splits, static_cast<unsigned>((ngrid + 255) / 256), 256, 0, c->d_partial.p, nsplit, ngrid,
-                                                                                    c->d_ivec.p);
-  INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaEventRecord(e2, c->stream));
   INCA_CUDA(c, cudaEventSynchronize(e2));
   float a = 0, b = 0;
@@ -142,8 +158,8 @@ int eval_device(inca_ctx* c, int mode, double tol) {
   cudaEventElapsedTime(&b, e0, e2);
   c->t_kernel_ms = a;
   c->t_total_ms = b;
-  c->t_kernel_launches = 1;
-  c->t_launches = 2;
+  c->t_kernel_launches = launches / 2;
+  c->t_launches = launches;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);

@@ -850,10 +850,12 @@ k_pass2(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
 }
 
 // ---------------------------------------------------------------- grid preparation
-// Morton keys of the points g = j * stride, j < n (stride 1: the whole grid).
+// Morton keys of the points g = j * stride, j < n (stride 1: the whole grid). With pmol (a
+// batch) the molecule occupies the top 7 bits and each coordinate 19 bits, so the sort keeps
+// every molecule's points together.
 __global__ void k_morton(int64_t n, int64_t stride, const double* __restrict__ px, const double* __restrict__ py,
-                         const double* __restrict__ pz, double lo0, double lo1, double lo2, double inv,
-                         uint64_t* key, int64_t* idx) {
+                         const double* __restrict__ pz, const int* __restrict__ pmol, double lo0, double lo1,
+                         double lo2, double inv, uint64_t* key, int64_t* idx) {
   const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (j >= n) return;
   const int64_t g = j * stride;
@@ -861,8 +863,10 @@ __global__ void k_morton(int64_t n, int64_t stride, const double* __restrict__ p
   uint64_t k = 0;
   uint32_t q[3];
   for (int d = 0; d < 3; ++d) q[d] = static_cast<uint32_t>(fmin(fmax(c[d], 0.0), 2097151.0));
-  for (int b = 20; b >= 0; --b)
+  const int low = pmol ? 2 : 0;
+  for (int b = 20; b >= low; --b)
     for (int d = 0; d < 3; ++d) k = (k << 1) | ((q[d] >> b) & 1u);
+  if (pmol) k |= static_cast<uint64_t>(pmol[g]) << 57;
   key[j] = k;
   idx[j] = g;
 }
@@ -1107,13 +1111,25 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
                 DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, DevBuf<TileInfo>& tiles,
                 int64_t* n_out, int64_t* ntiles_out) {
   const int64_t n = (c->ngrid + stride - 1) / stride;
-  const int64_t nwt = (n + kWarpTile - 1) / kWarpTile;
+  // tiles of <= 128 consecutive sorted points; in a batch they never straddle two molecules
+  std::vector<TileInfo> ht;
+  const bool batch = c->batch_molecules > 0;
+  const int nmol = batch ? c->batch_molecules : 1;
+  int64_t o = 0;
+  for (int m = 0; m < nmol; ++m) {
+    int64_t cnt = n;
+    if (batch) {  // sampled points of molecule m: multiples of stride in [off_m, off_m+1)
+      const int64_t a = c->h_mol_off[m], b = c->h_mol_off[m + 1];
+      cnt = (b + stride - 1) / stride - (a + stride - 1) / stride;
+    }
+    for (int64_t t = 0; t < cnt; t += kWarpTile)
+      ht.push_back(TileInfo{o + t, static_cast<int>(std::min<int64_t>(kWarpTile, cnt - t)), m});
+    o += cnt;
+  }
+  const int64_t nwt = static_cast<int64_t>(ht.size());
   if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT) ||
       tiles.reserve(std::max<int64_t>(nwt, 1)))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
-  std::vector<TileInfo> ht(nwt);
-  for (int64_t t = 0; t < nwt; ++t)
-    ht[t] = TileInfo{t * kWarpTile, static_cast<int>(std::min<int64_t>(kWarpTile, n - t * kWarpTile)), 0};
   if (nwt) INCA_CUDA(c, cudaMemcpy(tiles.p, ht.data(), sizeof(TileInfo) * nwt, cudaMemcpyHostToDevice));
   DevBuf<uint64_t> k1, k2;
   DevBuf<int64_t> i1;
@@ -1123,8 +1139,8 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
     rel();
     return set_error(c, INCA_E_NOMEM, "morton sort");
   }
-  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p, lo[0], lo[1], lo[2], inv,
-              k1.p, i1.p);
+  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p,
+              batch ? c->d_pmol.p : nullptr, lo[0], lo[1], lo[2], inv, k1.p, i1.p);
   size_t tb = 0;
   cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
   if (!e) e = tmp.reserve(tb);
@@ -1295,7 +1311,7 @@ int eval_mixed(inca_ctx* c, double eps) {
     Dpt = cv.take<double>(fused ? ngrid : 1);
     stats = cv.take<unsigned long long>(16);
     work = cv.take<unsigned long long>(4);
-    mchunks = cv.take<ChunkRange>(1);
+    mchunks = cv.take<ChunkRange>(c->mol_chunks.size());
     dmax = cv.take<unsigned long long>(2);
     errw = cv.take<int>(4);
     tab = cv.take<float2>(kExpTab + 1);
@@ -1326,8 +1342,8 @@ int eval_mixed(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
   INCA_CUDA(c, cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), c->stream));
-  const ChunkRange all_chunks{0, nchunks};
-  INCA_CUDA(c, cudaMemcpyAsync(mchunks, &all_chunks, sizeof(ChunkRange), cudaMemcpyHostToDevice, c->stream));
+  INCA_CUDA(c, cudaMemcpyAsync(mchunks, c->mol_chunks.data(), sizeof(ChunkRange) * c->mol_chunks.size(),
+                               cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(errw, 0, 4 * sizeof(int), c->stream));
   if (!off.empty())
     INCA_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
@@ -1400,7 +1416,9 @@ int eval_mixed(inca_ctx* c, double eps) {
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, q1, nullptr, Iss);
     INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, qabs, nullptr, Mss);
     std::vector<double> segTheta(nseg, 0.0);
-    const double nq = static_cast<double>(std::max<int64_t>(c->nsurv, 1));
+    // survivors of the largest molecule: an upper bound on the terms left out at a point
+    const double nq = static_cast<double>(
+        std::max<int64_t>(*std::max_element(c->mol_surv.begin(), c->mol_surv.end()), 1));
     int emode = 0;
     if (mode == 0) {
       INCA_CUDA(c, cudaMemsetAsync(Ios, 0, sizeof(double) * ngrid, c->stream));

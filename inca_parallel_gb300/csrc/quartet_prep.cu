@@ -32,7 +32,7 @@ struct PrepConst {
   double gh_node[kMaxGH + 1][kMaxGH];
   double gh_w[kMaxGH + 1][kMaxGH];
   double pi15;
-  double lim;
+  double thresh;
   double c_u;  // sqrt(1/ln 2): u = c_u r' turns e^(-r'^2) into 2^(-u^2)
   int nprim;
   int normalize;
@@ -191,10 +191,11 @@ __device__ int prepare_one(const PrimD* prims, int4 q, double v, QRec* out, doub
   }
   const double Jik = ja8(Pi, Pk, Rik2, aik, eik);
   const double Jjl = ja8(Pj, Pl, Rjl2, ajl, ejl);
+  const double lim = cP.thresh * Pi.lim_scale;
   const double screen1 = fabs(DMval) * sqrt(Jik * Jjl);
   *s1o = screen1;
   *s2o = 0.0;
-  if (!(screen1 >= cP.lim)) return 0;
+  if (!(screen1 >= lim)) return 0;
   const double zeta = aik + ajl;
   const double eijkl = (aik * ajl) * (1.0 / zeta);
   const double sqe = sqrt(eijkl);
@@ -221,7 +222,7 @@ __device__ int prepare_one(const PrimD* prims, int4 q, double v, QRec* out, doub
   }
   const double screen2 = fabs(((A * U[0]) * U[1]) * U[2]);
   *s2o = screen2;
-  if (!(screen2 >= cP.lim)) return 1;
+  if (!(screen2 >= lim)) return 1;
   out->A = A;
   out->sqe = sqe;
 #pragma unroll
@@ -272,7 +273,8 @@ __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl,
   flags[q] = static_cast<uint8_t>(f);
   if (s1) s1[q] = a1;
   if (s2) s2[q] = a2;
-  key[q] = (f == 3) ? class_key(rec.L) : 0xFFFFFFFFu;
+  // sort key: molecule (batches), then angular class; quartets that fail screening sort last
+  key[q] = (f == 3) ? (static_cast<uint32_t>(prims[r.x - 1].mol) << 16) | class_key(rec.L) : 0xFFFFFFFFu;
   return f;
 }
 
@@ -400,11 +402,11 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
       hc.gh_w[n][h] = inca_gh::kWeight[n][h];
     }
   hc.pi15 = pi * std::sqrt(pi);
-  hc.lim = thresh * (1.0 / (double(c->nprim) * (double(c->nprim) + 1.0) * 0.5));
+  hc.thresh = thresh;
   hc.c_u = std::sqrt(1.0 / std::log(2.0));
   hc.nprim = c->nprim;
   hc.normalize = normalize ? 1 : 0;
-  c->lim = hc.lim;
+  c->lim = thresh * (1.0 / (double(c->nprim) * (double(c->nprim) + 1.0) * 0.5));
   INCA_CUDA(c, cudaMemcpyToSymbolAsync(cP, &hc, sizeof(hc), 0, cudaMemcpyHostToDevice, c->stream));
 
   const int64_t n = c->nq;
@@ -438,11 +440,11 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   }
   size_t tmp_bytes = 0;
   if (e == cudaSuccess)
-    e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 15, c->stream);
+    e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 32, c->stream);
   DevBuf<unsigned char> tmp;
   if (e == cudaSuccess) e = tmp.reserve(tmp_bytes);
   if (e == cudaSuccess)
-    e = cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 15, c->stream);
+    e = cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 32, c->stream);
   // class histogram from the sorted keys: copy keys to host (4 B per quartet) is too
   // large for big lists, so run-length encode on the device.
   DevBuf<uint32_t> ukeys;
@@ -487,6 +489,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   for (int r = 0; r < h_runs; ++r) {
     if (hk[r] == 0xFFFFFFFFu) continue;
     ClassSeg s;
+    s.mol = static_cast<int>(hk[r] >> 16);
     s.L[0] = (hk[r] >> 10) & 31;
     s.L[1] = (hk[r] >> 5) & 31;
     s.L[2] = hk[r] & 31;
@@ -497,7 +500,6 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     s.count = hcnt[r];
     s.off64 = off64;
     s.off32 = off32;
-    s.pad = 0;
     off64 += s.count * s.stride;
     off32 += s.count * s.stride32;
     nsurv += s.count;
@@ -506,9 +508,24 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   }
   c->nsurv = nsurv;
   c->max_L = maxL;
-  // work chunks of <= 32 records within a class
+  // work chunks of <= 32 records within a class; each molecule's chunks are contiguous
   c->chunks.clear();
-  for (int s = 0; s < static_cast<int>(c->classes.size()); ++s)
+  const int nmol = std::max(c->batch_molecules, 1);
+  c->mol_chunks.assign(nmol, ChunkRange{0, 0});
+  c->mol_surv.assign(nmol, 0);
+  std::vector<bool> seen(nmol, false);
+  for (int s = 0; s < static_cast<int>(c->classes.size()); ++s) {
+    const int mol = c->classes[s].mol;
+    if (mol < 0 || mol >= nmol) {
+      cleanup();
+      tmp.release();
+      return set_error(c, INCA_E_STATE, "inca_prepare: molecule index outside the batch");
+    }
+    if (!seen[mol]) {
+      seen[mol] = true;
+      c->mol_chunks[mol].begin = static_cast<int>(c->chunks.size());
+    }
+    c->mol_surv[mol] += c->classes[s].count;
     for (int64_t f = 0; f < c->classes[s].count; f += 32) {
       WorkChunk w;
       w.cls = s;
@@ -516,6 +533,10 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
       w.rec = c->classes[s].first + f;
       c->chunks.push_back(w);
     }
+    c->mol_chunks[mol].end = static_cast<int>(c->chunks.size());
+  }
+  for (int m = 0; m < nmol; ++m)
+    if (!seen[m]) c->mol_chunks[m] = ChunkRange{0, 0};
   e = cudaSuccess;
   if (c->d_rec64.reserve(std::max<int64_t>(off64, 2)) || c->d_rec32.reserve(std::max<int64_t>(off32, 4)) ||
       c->d_surv_src.reserve(std::max<int64_t>(nsurv, 1)) ||
@@ -571,7 +592,7 @@ __device__ __forceinline__ double gam(const double* D, int n, int i, int k, int 
          0.5 * D[i + static_cast<int64_t>(n) * l] * D[j + static_cast<int64_t>(n) * k];
 }
 
-__global__ void k_closed_shell(int64_t nrec, int n, int64_t npair, int unique, const double* D,
+__global__ void k_closed_shell(int64_t nrec, int n, int64_t npair, int unique, const double* D, int base,
                                int4* ijkl, double* v) {
   const int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (r >= nrec) return;
@@ -595,32 +616,43 @@ __global__ void k_closed_shell(int64_t nrec, int n, int64_t npair, int unique, c
   for (int a = 0; a < nik; ++a)
     for (int b = 0; b < njl; ++b) s += gam(D, n, ik[a][0], ik[a][1], jl[b][0], jl[b][1]);
   if (unique && pa != pb) s *= 2.0;  // Gamma_{ik,jl} + Gamma_{jl,ik}
-  ijkl[r] = make_int4(i + 1, j + 1, k + 1, l + 1);
+  ijkl[r] = make_int4(base + i + 1, base + j + 1, base + k + 1, base + l + 1);
   v[r] = s;
 }
 }  // namespace
+
+int64_t closed_shell_records(int n, int unique) {
+  const int64_t npair = static_cast<int64_t>(n) * (n + 1) / 2;
+  return unique ? npair * (npair + 1) / 2 : npair * npair;
+}
+
+// Records of one molecule's closed-shell DM2 (n primitives, 1-RDM D) into the context's quartet
+// arrays at record offset `at`, with primitive indices offset by `base` (batches).
+int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int base, int64_t at) {
+  const int64_t npair = static_cast<int64_t>(n) * (n + 1) / 2;
+  const int64_t nrec = closed_shell_records(n, unique);
+  DevBuf<double> dD;
+  if (dD.reserve(static_cast<size_t>(n) * n)) return set_error(c, INCA_E_NOMEM, "D");
+  cudaError_t e = cudaMemcpyAsync(dD.p, D, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && nrec > 0) {
+    INCA_LAUNCH(c, k_closed_shell, static_cast<unsigned>((nrec + 255) / 256), 256, 0, nrec, n, npair, unique, dD.p,
+                base, c->d_ijkl.p + at, c->d_v.p + at);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  dD.release();
+  if (e != cudaSuccess) return cuda_error(c, e, "closed-shell DM2");
+  return INCA_OK;
+}
 
 int gen_closed_shell_device(inca_ctx* c, const double* D, int unique, int64_t* nrec_out) {
   if (c->nprim <= 0) return set_error(c, INCA_E_STATE, "primitives not set");
   if (!D) return set_error(c, INCA_E_ARG, "D is null");
   const int n = c->nprim;
-  const int64_t npair = static_cast<int64_t>(n) * (n + 1) / 2;
-  const int64_t nrec = unique ? npair * (npair + 1) / 2 : npair * npair;
-  DevBuf<double> dD;
-  if (dD.reserve(static_cast<size_t>(n) * n)) return set_error(c, INCA_E_NOMEM, "D");
-  if (c->d_ijkl.reserve(nrec) || c->d_v.reserve(nrec)) {
-    dD.release();
-    return set_error(c, INCA_E_NOMEM, "quartet records");
-  }
-  cudaError_t e = cudaMemcpyAsync(dD.p, D, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) {
-    INCA_LAUNCH(c, k_closed_shell, static_cast<unsigned>((nrec + 255) / 256), 256, 0, nrec, n, npair, unique, dD.p,
-                                                                                     c->d_ijkl.p, c->d_v.p);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  dD.release();
-  if (e != cudaSuccess) return cuda_error(c, e, "inca_gen_closed_shell_dm2");
+  const int64_t nrec = closed_shell_records(n, unique);
+  if (c->d_ijkl.reserve(nrec) || c->d_v.reserve(nrec)) return set_error(c, INCA_E_NOMEM, "quartet records");
+  const int st = gen_closed_shell_into(c, n, D, unique, 0, 0);
+  if (st) return st;
   c->nq = nrec;
   c->prepared = false;
   c->evaluated = false;

@@ -184,6 +184,27 @@ int inca_kernel_launches(inca_ctx* ctx, int64_t* count);
 int inca_fp32_fma_peak(inca_ctx* ctx, double* tflops);
 
 /* ---------------------------------------------------------------------------------------
+ * Batches of molecules. No counterpart in the reference, which runs calculate_intracule once per
+ * molecule (one process each); a batch runs the radial_plot job (src/mod_intracule.f90:512-533)
+ * for up to INCA_MAX_BATCH molecules with one screening pass and one launch of each evaluation
+ * kernel. inca_batch_clear starts a batch; inca_batch_add_closed_shell appends a molecule (its
+ * primitives as for inca_set_primitives, its closed-shell 1-RDM D(nprim,nprim) as for
+ * inca_gen_closed_shell_dm2, and its radial-scan grid as for inca_grid_scan; nradi returns the
+ * molecule's shell count); inca_batch_prepare generates and screens every molecule's DM2 and
+ * builds the concatenated grid (it replaces the context's primitives, quartets and grid;
+ * counts and ngrid, the total grid points, may be NULL); inca_batch_eval evaluates all molecules and writes their I(s)
+ * molecule after molecule into rintra (sum of the nradi values; NULL keeps them on the device).
+ * inca_eval and inca_radial_plot also work on a prepared batch. */
+#define INCA_MAX_BATCH 128
+int inca_batch_clear(inca_ctx* ctx);
+int inca_batch_add_closed_shell(inca_ctx* ctx, int32_t nprim, const double* alpha, const int32_t* tmn,
+                                const double* xn, const double* yn, const double* zn, const double* D,
+                                int unique, int32_t nblock, const double* start, const double* end,
+                                const double* step, const int32_t* nang, int nosym, int32_t* nradi);
+int inca_batch_prepare(inca_ctx* ctx, double thresh, inca_counts* counts, int64_t* ngrid);
+int inca_batch_eval(inca_ctx* ctx, int mode, double tol, double* rintra);
+
+/* ---------------------------------------------------------------------------------------
  * Evaluation without allocation. No counterpart in the reference (the Fortran program
  * allocates its work arrays itself); this entry point exists for callers that must not
  * allocate device memory while they run: a solver that keeps all its device memory in its

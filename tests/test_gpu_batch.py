@@ -1,0 +1,82 @@
+"""Batches of molecules (inca_batch_*): I(s) of every molecule from one batched evaluation
+against the same molecules evaluated one at a time.
+
+Tolerances: FP64 form 1e-12 relative per I(s) (only the split of the quartet sums differs);
+mixed form 1e-8 relative per I(s) against the per-molecule FP64 form; quartet counts equal to
+the sums of the per-molecule counts.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+THRESH = 1e-12
+SCAN = ([0.0], [5.0], [0.1], [302])
+
+
+@pytest.fixture(scope="module")
+def molecules():
+    from inca_parallel_gb300 import workloads as W
+    rng = np.random.default_rng(W.SEED0 + 3)
+    mols = []
+    for natoms, nprim in [(3, 24), (4, 30), (5, 36), (3, 20), (6, 40)]:
+        b = W.random_molecule(rng, natoms, nprim)
+        # s and p shells with exponents up to 50 (the polynomial fit of the reference is exact there)
+        keep = (b["tmn"].sum(1) <= 1) & (b["alpha"] <= 50.0)
+        b = {**b, "alpha": b["alpha"][keep], "tmn": b["tmn"][keep], "xyz": b["xyz"][keep]}
+        nocc = max(1, min(W.electrons(b) // 2, len(b["alpha"]) // 3))
+        D, _ = W.closed_shell_density(b, nocc, int(rng.integers(1 << 30)))
+        mols.append((b, D))
+    return mols
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from inca_parallel_gb300 import build
+    build.build()
+    from inca_parallel_gb300 import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def single(ctx, b, D, mode):
+    ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+    ctx.gen_closed_shell_dm2(D, unique=False)
+    counts = ctx.prepare(THRESH)
+    ctx.grid_scan(*SCAN)
+    ctx.eval(mode=mode, tol=1e-8)
+    return counts, ctx.radial_plot()[1]
+
+
+def test_batch_matches_single_molecules(ctx, molecules):
+    refs = [single(ctx, b, D, 0) for b, D in molecules]
+    ctx.batch_clear()
+    for b, D in molecules:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN)
+    counts = ctx.batch_prepare(THRESH)
+    assert tuple(counts) == tuple(int(sum(r[0][k] for r in refs)) for k in range(3))
+    assert ctx.ngrid >= 16384  # the one-pass mixed form
+    I64 = ctx.batch_eval(mode=0)
+    for (cnt, ref), got in zip(refs, I64):
+        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=0)
+    Imix = ctx.batch_eval(mode=1, tol=1e-8)
+    for (cnt, ref), got in zip(refs, Imix):
+        np.testing.assert_allclose(got, ref, rtol=1e-8, atol=0)
+    # deterministic
+    again = ctx.batch_eval(mode=1, tol=1e-8)
+    for a, b_ in zip(Imix, again):
+        np.testing.assert_array_equal(a, b_)
+
+
+def test_batch_errors(ctx, molecules):
+    from inca_parallel_gb300 import IncaError
+    ctx.batch_clear()
+    with pytest.raises(IncaError, match="INCA_E_STATE"):
+        ctx.batch_prepare(THRESH)
+    b, D = molecules[0]
+    ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN)
+    ctx.batch_prepare(THRESH)
+    ctx.grid_scan(*SCAN)  # replaces the batch grid
+    with pytest.raises(IncaError, match="INCA_E_STATE"):
+        ctx.batch_eval(mode=0)
