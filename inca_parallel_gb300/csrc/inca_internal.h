@@ -84,6 +84,25 @@ struct ChunkRange {
   int begin, end;
 };
 
+// Work of one molecule in a persistent pass: its chunk range, its quartet splits, its tiles
+// and sorted points, where its work items start, and where its partial sums and left-out
+// bound masses start (partials: split-major over the molecule's points; masses: split-major
+// over its tiles).
+struct MolWork {
+  int cb, ce;
+  int nsplit;
+  int pad;
+  int64_t tile0, ntiles;
+  int64_t p0, np;
+  int64_t item0;
+  int64_t poff, doff;
+};
+
+// Tiles and sorted points of one molecule in a sorted grid.
+struct MolSpan {
+  int64_t tile0, ntiles, p0, np;
+};
+
 // One molecule of a batch, as added (host copies until the batch is prepared).
 struct BatchMol {
   int nprim = 0;
@@ -165,6 +184,7 @@ struct inca_ctx {
   inca::DevBuf<float> d_wtbox;        // per 128-point warp tile: lo[3], hi[3], 2 pad
   inca::DevBuf<inca::TileInfo> d_tiles;  // tiles of the sorted grid
   int64_t ntiles = 0;
+  std::vector<inca::MolSpan> mol_span;   // per molecule: its tiles and sorted points
   // the same for a strided sample of the grid (threshold estimates of the one-pass form)
   int64_t sample_version = -1;
   int64_t nsample = 0;
@@ -173,6 +193,7 @@ struct inca_ctx {
   inca::DevBuf<float> d_wtbox_s;
   inca::DevBuf<inca::TileInfo> d_tiles_s;
   int64_t ntiles_s = 0;
+  std::vector<inca::MolSpan> mol_span_s;
   inca::DevBuf<unsigned char> d_scratch_s;
 
   // scratch

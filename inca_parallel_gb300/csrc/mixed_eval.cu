@@ -521,6 +521,33 @@ __device__ __forceinline__ void stage_first(const Stage& S, const WorkChunk* chu
   }
 }
 
+// The molecule owning a work item / sorted point / tile: the last entry whose start is <= x
+// (molecules without work share their start with the next one and are never returned).
+__device__ __forceinline__ int mol_of_item(const MolWork* __restrict__ mw, int nmol, int64_t x) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mw[mid].item0 <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int mol_of_point(const MolWork* __restrict__ mw, int nmol, int64_t x) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mw[mid].p0 <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int mol_of_tile(const MolWork* __restrict__ mw, int nmol, int64_t x) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mw[mid].tile0 <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Next work item of a persistent CTA: (tile, split) pairs, taken from a device counter.
 __device__ __forceinline__ int64_t next_item(unsigned long long* work) {
   unsigned long long it = 0;
@@ -552,10 +579,10 @@ __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chun
 //   so the lanes run the same instruction sequence on different quartets).
 template <bool kFuse>
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
-k_pass1(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol_chunks,
+k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
-        int64_t ntiles, int nsplit, int64_t ngrid, int stage_floats, const float* __restrict__ pt_tau,
+        int64_t nitems, int stage_floats, const float* __restrict__ pt_tau,
         const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop, double* __restrict__ part,
         double* __restrict__ part_abs, double* __restrict__ drop_mass, unsigned long long* __restrict__ work,
         unsigned long long* __restrict__ stats, int* __restrict__ err) {
@@ -568,15 +595,25 @@ k_pass1(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
   stage_init(S);
   unsigned long long nskip = 0, nlive = 0, ncorr = 0, nround = 0;
   int k = 0;  // chunks taken by this CTA so far: selects buffer and barrier phase
-  const int64_t nitems = ntiles * nsplit;
   for (;;) {
     const int64_t item = next_item(work);
     if (item >= nitems) break;
-    const int64_t wtile = item / nsplit;
-    const int split = static_cast<int>(item - wtile * nsplit);
+    int64_t wtile, pat, dat;
+    int nsplit, first;
+    ChunkRange cr;
+    {
+      const MolWork& W = mw[mol_of_item(mw, nmol, item)];
+      const int64_t local = item - W.item0;
+      const int64_t tl = local / W.nsplit;
+      const int split = static_cast<int>(local - tl * W.nsplit);
+      nsplit = W.nsplit;
+      wtile = W.tile0 + tl;
+      cr = ChunkRange{W.cb, W.ce};
+      first = cr.begin + split;
+      pat = W.poff + static_cast<int64_t>(split) * W.np - W.p0;  // + sorted point index
+      dat = W.doff + static_cast<int64_t>(split) * W.ntiles + tl;
+    }
     const TileInfo T = tiles[wtile];
-    const ChunkRange cr = mol_chunks[T.mol];
-    const int first = cr.begin + split;
     if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
     float rh[3][kPPT], rl[3][kPPT];
     load_points(phi, plo, T, lane, rh, rl);
@@ -700,14 +737,14 @@ k_pass1(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
       if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
       const int j = lane + 32 * p;
       if (j < T.count) {
-        part[static_cast<int64_t>(split) * ngrid + T.start + j] = acc[p];
-        part_abs[static_cast<int64_t>(split) * ngrid + T.start + j] = static_cast<double>(sa[p]);
+        part[pat + T.start + j] = acc[p];
+        part_abs[pat + T.start + j] = static_cast<double>(sa[p]);
       }
     }
     if (kFuse && drop_mass) {
       for (int o = 16; o > 0; o >>= 1) dm += __shfl_xor_sync(0xffffffffu, dm, o);
       // the FP32 sum of the left-out bounds, raised by a margin for its own rounding
-      if (lane == 0) drop_mass[static_cast<int64_t>(split) * ntiles + wtile] = dm * 1.0001;
+      if (lane == 0) drop_mass[dat] = dm * 1.0001;
     }
   }
   if (kFuse)
@@ -724,12 +761,12 @@ k_pass1(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
 
 // ---------------------------------------------------------------- pass 2 (corrections)
 __global__ void __launch_bounds__(32, 16)
-k_pass2(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol_chunks,
+k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
         const float* __restrict__ gbox, const float* __restrict__ g_lt, const float* __restrict__ pt_tau,
         const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop, const float2* __restrict__ exp_tab,
-        int64_t ntiles, int nsplit, int64_t ngrid, int stage_floats, double* __restrict__ part,
+        int64_t nitems, int stage_floats, double* __restrict__ part,
         unsigned long long* __restrict__ work, unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
@@ -739,14 +776,23 @@ k_pass2(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
   stage_init(S);
   unsigned long long n32 = 0, ndf = 0, npts = 0;
   int k = 0;
-  const int64_t nitems = ntiles * nsplit;
   for (;;) {
     const int64_t item = next_item(work);
     if (item >= nitems) break;
-    const int64_t wtile = item / nsplit;
-    const int split = static_cast<int>(item - wtile * nsplit);
+    int64_t wtile, pat;
+    int nsplit, split;
+    ChunkRange cr;
+    {
+      const MolWork& W = mw[mol_of_item(mw, nmol, item)];
+      const int64_t local = item - W.item0;
+      const int64_t tl = local / W.nsplit;
+      split = static_cast<int>(local - tl * W.nsplit);
+      nsplit = W.nsplit;
+      wtile = W.tile0 + tl;
+      cr = ChunkRange{W.cb, W.ce};
+      pat = W.poff + static_cast<int64_t>(split) * W.np - W.p0;
+    }
     const TileInfo T = tiles[wtile];
-    const ChunkRange cr = mol_chunks[T.mol];
     // a tile none of whose sub-tiles can need a correction contributes zeros
     bool any_sub = false;
 #pragma unroll
@@ -839,7 +885,7 @@ k_pass2(const WorkChunk* __restrict__ chunks, const ChunkRange* __restrict__ mol
     for (int p = 0; p < kPPT; ++p) {
       acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
       const int j = lane + 32 * p;
-      if (j < T.count) part[static_cast<int64_t>(split) * ngrid + T.start + j] = acc[p];
+      if (j < T.count) part[pat + T.start + j] = acc[p];
     }
   }
   if (lane == 0) {
@@ -1034,18 +1080,6 @@ __global__ void k_absmax2(int64_t n, const double* __restrict__ I, const double*
   }
 }
 
-// Sum the split partials of the passes (sorted order) in a fixed order.
-__global__ void k_sum_splits(int64_t n, int nsplit, const double* __restrict__ a, const double* __restrict__ b,
-                             double* out) {
-  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (i >= n) return;
-  double s = 0.0;
-  for (int k = 0; k < nsplit; ++k) s += a[static_cast<int64_t>(k) * n + i];
-  if (b)
-    for (int k = 0; k < nsplit; ++k) s += b[static_cast<int64_t>(k) * n + i];
-  out[i] = s;
-}
-
 __global__ void k_scatter(int64_t n, const int64_t* __restrict__ perm, const double* __restrict__ src, double* dst) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i < n) dst[perm[i]] = src[i];
@@ -1103,27 +1137,56 @@ __global__ void k_tile_to_points(const TileInfo* __restrict__ tiles, int64_t nwt
   for (int j = lane; j < T.count; j += 32) out[perm[T.start + j]] = vt[wt];
 }
 
+// Sum over the splits of each sorted point (partials laid out per molecule), in split order;
+// b (optional) has the same layout and is added after a.
+__global__ void k_sum_mol(int64_t n, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ a,
+                          const double* __restrict__ b, double* out) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const MolWork W = mw[mol_of_point(mw, nmol, i)];
+  const int64_t at = W.poff + (i - W.p0);
+  double s = 0.0;
+  for (int k = 0; k < W.nsplit; ++k) s += a[at + static_cast<int64_t>(k) * W.np];
+  if (b)
+    for (int k = 0; k < W.nsplit; ++k) s += b[at + static_cast<int64_t>(k) * W.np];
+  out[i] = s;
+}
+
+// Left-out bound mass of each tile: sum over its molecule's splits.
+__global__ void k_sum_drop(int64_t ntiles, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ d,
+                           double* out) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= ntiles) return;
+  const MolWork W = mw[mol_of_tile(mw, nmol, t)];
+  double s = 0.0;
+  for (int k = 0; k < W.nsplit; ++k) s += d[W.doff + static_cast<int64_t>(k) * W.ntiles + (t - W.tile0)];
+  out[t] = s;
+}
+
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
 // permutation (sorted position -> grid index) and the tile / sub-tile boxes.
 int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, DevBuf<float4>& phi,
                 DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, DevBuf<TileInfo>& tiles,
-                int64_t* n_out, int64_t* ntiles_out) {
+                int64_t* n_out, int64_t* ntiles_out, std::vector<MolSpan>& spans) {
   const int64_t n = (c->ngrid + stride - 1) / stride;
   // tiles of <= 128 consecutive sorted points; in a batch they never straddle two molecules
   std::vector<TileInfo> ht;
   const bool batch = c->batch_molecules > 0;
   const int nmol = batch ? c->batch_molecules : 1;
   int64_t o = 0;
+  spans.assign(nmol, MolSpan{0, 0, 0, 0});
   for (int m = 0; m < nmol; ++m) {
     int64_t cnt = n;
     if (batch) {  // sampled points of molecule m: multiples of stride in [off_m, off_m+1)
       const int64_t a = c->h_mol_off[m], b = c->h_mol_off[m + 1];
       cnt = (b + stride - 1) / stride - (a + stride - 1) / stride;
     }
+    spans[m] = MolSpan{static_cast<int64_t>(ht.size()), 0, o, cnt};
     for (int64_t t = 0; t < cnt; t += kWarpTile)
       ht.push_back(TileInfo{o + t, static_cast<int>(std::min<int64_t>(kWarpTile, cnt - t)), m});
+    spans[m].ntiles = static_cast<int64_t>(ht.size()) - spans[m].tile0;
     o += cnt;
   }
   const int64_t nwt = static_cast<int64_t>(ht.size());
@@ -1180,13 +1243,13 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
   int64_t nn = 0;
   if (!main_ok) {
     const int st = sort_points(c, 1, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
-                               &c->ntiles);
+                               &c->ntiles, c->mol_span);
     if (st) return st;
     c->mix_version = c->grid_version;
   }
   if (!sample_ok) {
     const int st = sort_points(c, kSampleStride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
-                               c->d_tiles_s, &c->nsample, &c->ntiles_s);
+                               c->d_tiles_s, &c->nsample, &c->ntiles_s, c->mol_span_s);
     if (st) return st;
     c->sample_version = c->grid_version;
   }
@@ -1225,13 +1288,35 @@ std::vector<float2> exp2_table() {
   return t;
 }
 
-// Quartet splits per tile: enough (tile, split) work items for kItemsPerCta items per resident
-// CTA, so that the persistent CTAs finish together (an item is small next to the whole).
-int item_splits(int64_t ntiles, int64_t nchunks, int num_sms) {
-  const int64_t target = static_cast<int64_t>(num_sms) * INCA_PASS_CTAS_PER_SM * kItemsPerCta;
-  int64_t s = (target + std::max<int64_t>(ntiles, 1) - 1) / std::max<int64_t>(ntiles, 1);
-  s = std::max<int64_t>(1, std::min<int64_t>(s, std::max<int64_t>(nchunks, 1)));
-  return static_cast<int>(std::min<int64_t>(s, 4096));
+// Work table of a persistent pass over a sorted grid: each molecule's quartet splits in
+// proportion to its tiles x chunks, about kItemsPerCta work items per resident CTA in total
+// (an item is then small next to the whole pass, so the CTAs finish together).
+std::vector<MolWork> work_table(const std::vector<MolSpan>& sp, const std::vector<ChunkRange>& ch, int num_sms,
+                                int64_t* nitems, int64_t* npart, int64_t* ndrop) {
+  const int nmol = static_cast<int>(sp.size());
+  const double target = double(num_sms) * INCA_PASS_CTAS_PER_SM * kItemsPerCta;
+  double total = 0.0;
+  for (int m = 0; m < nmol; ++m) total += double(sp[m].ntiles) * std::max(ch[m].end - ch[m].begin, 0);
+  std::vector<MolWork> w(nmol);
+  int64_t it = 0, po = 0, dro = 0;
+  for (int m = 0; m < nmol; ++m) {
+    const int nch = std::max(ch[m].end - ch[m].begin, 0);
+    int64_t ns = 1;
+    if (sp[m].ntiles > 0 && nch > 0 && total > 0.0) {
+      const double items = target * double(sp[m].ntiles) * nch / total;
+      ns = std::llround(items / double(sp[m].ntiles));
+      ns = std::max<int64_t>(1, std::min<int64_t>(ns, std::min(nch, 4096)));
+    }
+    w[m] = MolWork{ch[m].begin, ch[m].end, static_cast<int>(ns), 0, sp[m].tile0, sp[m].ntiles, sp[m].p0, sp[m].np,
+                   it, po, dro};
+    it += sp[m].ntiles * ns;
+    po += ns * sp[m].np;
+    dro += ns * sp[m].ntiles;
+  }
+  *nitems = it;
+  *npart = po;
+  *ndrop = dro;
+  return w;
 }
 
 // Resident CTAs of a persistent pass launch (one-warp CTAs, INCA_PASS_CTAS_PER_SM per SM).
@@ -1260,8 +1345,10 @@ int eval_mixed(inca_ctx* c, double eps) {
   if (st) return st;
   const int64_t nwt = c->ntiles;
   const int64_t ngroups = nwt * kPPT;
-  const int nsplit = item_splits(nwt, nchunks, c->num_sms);
-  const unsigned nctas = persistent_ctas(nwt * nsplit, c->num_sms);
+  int64_t nitems = 0, npart = 0, ndrop = 0;
+  const std::vector<MolWork> hmw = work_table(c->mol_span, c->mol_chunks, c->num_sms, &nitems, &npart, &ndrop);
+  const int nmol = static_cast<int>(hmw.size());
+  const unsigned nctas = persistent_ctas(nitems, c->num_sms);
   const float* wbox = c->d_wtbox.p;
   const float* gbox = c->d_wtbox.p + 8 * nwt;
   const TileInfo* tiles = c->d_tiles.p;
@@ -1284,19 +1371,19 @@ int eval_mixed(inca_ctx* c, double eps) {
   }
   const int nseg = off.empty() ? 1 : static_cast<int>(off.size()) - 1;
 
-  // scratch: pass sums and error-bound sums (nsplit x n), I~ / E~ sorted and grid order,
+  // scratch: pass sums and error-bound sums (per molecule: splits x points), I~ / E~ sorted and grid order,
   // thresholds, left-out bound mass per tile, statistics, the exp table, segment sums
   double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT, *dmass, *Dt, *Dpt;
   float *glt, *ptau, *ptau_est, *ptheta, *ltdrop;
   unsigned long long *stats, *dmax, *work;
-  ChunkRange* mchunks;
+  MolWork* mwdev;
   int* errw;
   int64_t* doff;
   float2* tab;
   auto layout = [&](Carve& cv) {
-    p1 = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
-    pabs = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
-    p2 = cv.take<double>(static_cast<size_t>(nsplit) * ngrid);
+    p1 = cv.take<double>(npart);
+    pabs = cv.take<double>(npart);
+    p2 = cv.take<double>(npart);
     Is = cv.take<double>(ngrid);
     Ms = cv.take<double>(ngrid);
     Io = cv.take<double>(ngrid);
@@ -1306,12 +1393,12 @@ int eval_mixed(inca_ctx* c, double eps) {
     ptau_est = cv.take<float>(fused ? ngrid : 1);
     ptheta = cv.take<float>(fused ? ngrid : 1);
     ltdrop = cv.take<float>(fused ? nwt : 1);
-    dmass = cv.take<double>(fused ? static_cast<size_t>(nsplit) * nwt : 1);
+    dmass = cv.take<double>(fused ? ndrop : 1);
     Dt = cv.take<double>(fused ? nwt : 1);
     Dpt = cv.take<double>(fused ? ngrid : 1);
     stats = cv.take<unsigned long long>(16);
     work = cv.take<unsigned long long>(4);
-    mchunks = cv.take<ChunkRange>(c->mol_chunks.size());
+    mwdev = cv.take<MolWork>(nmol);
     dmax = cv.take<unsigned long long>(2);
     errw = cv.take<int>(4);
     tab = cv.take<float2>(kExpTab + 1);
@@ -1342,8 +1429,7 @@ int eval_mixed(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
   INCA_CUDA(c, cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), c->stream));
-  INCA_CUDA(c, cudaMemcpyAsync(mchunks, c->mol_chunks.data(), sizeof(ChunkRange) * c->mol_chunks.size(),
-                               cudaMemcpyHostToDevice, c->stream));
+  INCA_CUDA(c, cudaMemcpyAsync(mwdev, hmw.data(), sizeof(MolWork) * nmol, cudaMemcpyHostToDevice, c->stream));
   INCA_CUDA(c, cudaMemsetAsync(errw, 0, 4 * sizeof(int), c->stream));
   if (!off.empty())
     INCA_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
@@ -1392,12 +1478,15 @@ int eval_mixed(inca_ctx* c, double eps) {
       if (end != env && v >= 0.0 && std::isfinite(v)) safety = v;
     }
     const int64_t ns = c->nsample;
-    const int64_t nwt_s = c->ntiles_s;
-    const int nsplit_s = item_splits(nwt_s, nchunks, c->num_sms);
+    int64_t nitems_s = 0, npart_s = 0, ndrop_s = 0;
+    const std::vector<MolWork> hmw_s =
+        work_table(c->mol_span_s, c->mol_chunks, c->num_sms, &nitems_s, &npart_s, &ndrop_s);
     double *q1, *qabs, *Iss, *Mss, *Ios, *Mos, *ws;
+    MolWork* mws;
     auto layout_s = [&](Carve& cs) {
-      q1 = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);
-      qabs = cs.take<double>(static_cast<size_t>(nsplit_s) * ns);
+      q1 = cs.take<double>(npart_s);
+      qabs = cs.take<double>(npart_s);
+      mws = cs.take<MolWork>(nmol);
       Iss = cs.take<double>(ns);
       Mss = cs.take<double>(ns);
       Ios = cs.take<double>(ngrid);
@@ -1409,12 +1498,13 @@ int eval_mixed(inca_ctx* c, double eps) {
     if (c->d_scratch_s.reserve(dry_s.off + 256)) return set_error(c, INCA_E_NOMEM, "sample scratch");
     Carve cs{c->d_scratch_s.p};
     layout_s(cs);
-    INCA_LAUNCH(c, k_pass1<false>, persistent_ctas(nwt_s * nsplit_s, c->num_sms), 32, dsmem, c->d_chunks.p, mchunks,
-                c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, nwt_s,
-                nsplit_s, ns, stage_floats, nullptr, nullptr, nullptr, q1, qabs, nullptr, work + 3, stats + 8, errw);
+    INCA_CUDA(c, cudaMemcpyAsync(mws, hmw_s.data(), sizeof(MolWork) * nmol, cudaMemcpyHostToDevice, c->stream));
+    INCA_LAUNCH(c, k_pass1<false>, persistent_ctas(nitems_s, c->num_sms), 32, dsmem, c->d_chunks.p, mws, nmol,
+                c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, nitems_s,
+                stage_floats, nullptr, nullptr, nullptr, q1, qabs, nullptr, work + 3, stats + 8, errw);
     INCA_CUDA(c, cudaGetLastError());
-    INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, q1, nullptr, Iss);
-    INCA_LAUNCH(c, k_sum_splits, nblk(ns), 256, 0, ns, nsplit_s, qabs, nullptr, Mss);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, mws, nmol, q1, nullptr, Iss);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, mws, nmol, qabs, nullptr, Mss);
     std::vector<double> segTheta(nseg, 0.0);
     // survivors of the largest molecule: an upper bound on the terms left out at a point
     const double nq = static_cast<double>(
@@ -1464,20 +1554,20 @@ int eval_mixed(inca_ctx* c, double eps) {
     // terms below the drop thresholds left out)
     INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
     if (fused)
-      INCA_LAUNCH(c, k_pass1<true>, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                  c->d_plo.p, tiles, wbox, nwt, nsplit, ngrid, stage_floats, ptau_est, tab, use_drop ? ltdrop : nullptr,
-                  p1, pabs, dmass, work, stats, errw);
+      INCA_LAUNCH(c, k_pass1<true>, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p,
+                  c->d_phi.p, c->d_plo.p, tiles, wbox, nitems, stage_floats, ptau_est, tab,
+                  use_drop ? ltdrop : nullptr, p1, pabs, dmass, work, stats, errw);
     else
-      INCA_LAUNCH(c, k_pass1<false>, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p,
-                  c->d_phi.p, c->d_plo.p, tiles, wbox, nwt, nsplit, ngrid, stage_floats, nullptr, nullptr, nullptr, p1,
-                  pabs, nullptr, work, stats, errw);
+      INCA_LAUNCH(c, k_pass1<false>, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p,
+                  c->d_phi.p, c->d_plo.p, tiles, wbox, nitems, stage_floats, nullptr, nullptr, nullptr, p1, pabs,
+                  nullptr, work, stats, errw);
     INCA_CUDA(c, cudaGetLastError());
     INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
-    INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, nullptr, Is);
-    INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, pabs, nullptr, Ms);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, p1, nullptr, Is);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, pabs, nullptr, Ms);
     INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
     if (use_drop) {
-      INCA_LAUNCH(c, k_sum_splits, nblk(nwt), 256, 0, nwt, nsplit, dmass, nullptr, Dt);
+      INCA_LAUNCH(c, k_sum_drop, nblk(nwt), 256, 0, nwt, mwdev, nmol, dmass, Dt);
       INCA_LAUNCH(c, k_tile_to_points, tblk, 256, 0, tiles, nwt, c->d_perm.p, Dt, Dpt);
     }
 
@@ -1531,13 +1621,13 @@ int eval_mixed(inca_ctx* c, double eps) {
   }
   INCA_CUDA(c, cudaEventRecord(ev.e[3], c->stream));
   if (run_pass2) {
-    INCA_LAUNCH(c, k_pass2, nctas, 32, dsmem, c->d_chunks.p, mchunks, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
+    INCA_LAUNCH(c, k_pass2, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
                 c->d_plo.p, tiles, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, use_drop ? ltdrop : nullptr, tab,
-                nwt, nsplit, ngrid, stage_floats, p2, work + 1, stats + 4, errw);
+                nitems, stage_floats, p2, work + 1, stats + 4, errw);
     INCA_CUDA(c, cudaGetLastError());
   }
   INCA_CUDA(c, cudaEventRecord(ev.e[4], c->stream));
-  INCA_LAUNCH(c, k_sum_splits, nblk(ngrid), 256, 0, ngrid, nsplit, p1, run_pass2 ? p2 : nullptr, Is);
+  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, p1, run_pass2 ? p2 : nullptr, Is);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, c->d_ivec.p);
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaEventRecord(ev.e[5], c->stream));
