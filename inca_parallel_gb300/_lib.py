@@ -19,6 +19,7 @@ STATUS = {0: "INCA_OK", 1: "INCA_E_ARG", 2: "INCA_E_CUDA", 3: "INCA_E_IO", 4: "I
           5: "INCA_E_STATE", 6: "INCA_E_NOMEM", 7: "INCA_E_LIMIT", 8: "INCA_E_TIMEOUT"}
 
 DP = ctypes.POINTER(ctypes.c_double)
+FP = ctypes.POINTER(ctypes.c_float)
 IP = ctypes.POINTER(ctypes.c_int32)
 I64P = ctypes.POINTER(ctypes.c_int64)
 U8P = ctypes.POINTER(ctypes.c_uint8)
@@ -58,6 +59,16 @@ SIGNATURES = {
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
     "inca_fp32_fma_peak": (ctypes.c_int, [VP, DP]),
+    "inca_mlp_create": (ctypes.c_int, [ctypes.POINTER(VP), ctypes.c_int, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, ctypes.c_uint64]),
+    "inca_mlp_destroy": (ctypes.c_int, [VP]),
+    "inca_mlp_param_count": (ctypes.c_int, [VP, I64P]),
+    "inca_mlp_get_params": (ctypes.c_int, [VP, FP]),
+    "inca_mlp_set_params": (ctypes.c_int, [VP, FP]),
+    "inca_mlp_forward": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP]),
+    "inca_mlp_gradient": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP, FP, FP]),
+    "inca_mlp_train": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                      ctypes.c_uint64, FP]),
     "inca_batch_clear": (ctypes.c_int, [VP]),
     "inca_batch_add_closed_shell": (ctypes.c_int, [VP, ctypes.c_int32, DP, IP, DP, DP, DP, DP, ctypes.c_int,
                                                    ctypes.c_int32, DP, DP, DP, IP, ctypes.c_int, IP]),
@@ -350,3 +361,68 @@ def centercalc(an, cartes, nohydro=True, betaone=False):
         raise IncaError(st, "inca_centercalc failed")
     n = nq.value
     return cent[:3 * n].reshape(n, 3), Ps[:n], sf[:n]
+
+
+class MLP:
+    """The library's multilayer perceptron (nin -> nhidden -> nhidden -> nout, tanh), trained
+    and evaluated on the GPU by its own kernels (include/inca_gpu.h, inca_mlp_*)."""
+
+    def __init__(self, nin, nhidden, nout, seed=1, device=0):
+        self.lib = load()
+        self.h = VP()
+        st = self.lib.inca_mlp_create(ctypes.byref(self.h), device, nin, nhidden, nout, seed)
+        if st:
+            raise IncaError(st, "inca_mlp_create")
+        self.nin, self.nh, self.nout = nin, nhidden, nout
+        n = ctypes.c_int64()
+        self.lib.inca_mlp_param_count(self.h, ctypes.byref(n))
+        self.nparam = n.value
+
+    def _check(self, st, what):
+        if st:
+            raise IncaError(st, what)
+
+    def close(self):
+        if self.h:
+            self.lib.inca_mlp_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(self.nparam, dtype=np.float32)
+        self._check(self.lib.inca_mlp_get_params(self.h, p.ctypes.data_as(FP)), "inca_mlp_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparam
+        self._check(self.lib.inca_mlp_set_params(self.h, p.ctypes.data_as(FP)), "inca_mlp_set_params")
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, self.nin)
+        Y = np.zeros((len(X), self.nout), dtype=np.float32)
+        self._check(self.lib.inca_mlp_forward(self.h, len(X), X.ctypes.data_as(FP), Y.ctypes.data_as(FP)),
+                    "inca_mlp_forward")
+        return Y
+
+    def gradient(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, self.nin)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, self.nout)
+        loss = ctypes.c_float()
+        g = np.zeros(self.nparam, dtype=np.float32)
+        self._check(self.lib.inca_mlp_gradient(self.h, len(X), X.ctypes.data_as(FP), T.ctypes.data_as(FP),
+                                               ctypes.byref(loss), g.ctypes.data_as(FP)), "inca_mlp_gradient")
+        return loss.value, g
+
+    def train(self, X, T, epochs, batch=256, lr=1e-3, seed=7):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, self.nin)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, self.nout)
+        loss = ctypes.c_float()
+        self._check(self.lib.inca_mlp_train(self.h, len(X), X.ctypes.data_as(FP), T.ctypes.data_as(FP), epochs, batch,
+                                            lr, seed, ctypes.byref(loss)), "inca_mlp_train")
+        return loss.value

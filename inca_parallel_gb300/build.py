@@ -31,6 +31,7 @@ UNITS = {
     "noalloc_eval.cu": [],
     "peak_probe.cu": [],
     "batch.cu": [],
+    "mlp.cu": [],
     "host_tables.cpp": [],
 }
 DRIVER_SRC = os.path.join(CSRC, "driver", "inca_main.cpp")

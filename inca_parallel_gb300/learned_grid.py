@@ -1,0 +1,213 @@
+"""Learned per-centre radial grids for the automatic multicentre grids.
+
+mod_autogrid (src/mod_autogrid.f90:12-185) puts integration centres at the origin and at the
+interatomic vectors R_j - R_k and gives each a radial map r = a (1 + x) / (1 - x) whose scale a
+comes from Bragg-Slater radii; every centre then gets the same nrad (mod_build_grid.f90:13-277).
+Near a centre the intracule is a sum of Gaussians whose exponents come from the primitives of
+the atoms behind the centre (e = 2 a_i a_j / (a_i + a_j) for primitives i on atom A and j on
+atom B: the product Gaussians of the quartet terms with (i, k) on A and (j, l) on B peak exactly
+at R_B - R_A). Bragg-Slater radii do not see those exponents.
+
+This module trains a small network -- the library's own GPU kernels, inca_mlp_* -- to predict
+for each centre (1) a multiplier of autogrid's scale and (2) the number of radial nodes, from
+geometry and exponent features. The training targets come from the one-dimensional problem each
+centre solves: for the centre's Gaussian components, the scale that minimises the relative
+Gauss-Legendre error of their radial integrals (int r^2 exp(-e r^2) dr over the mapped rule) at a
+given nrad, and the smallest nrad whose best error is below the target. Autogrid's centres and
+Ps stay; its scale and the caller's nrad stay the fallback where the features leave the training
+range or a prediction leaves its bounds. The judge of a grid is the radial integral against a
+dense reference grid (nrad 150, nang 974) computed by the engine itself.
+"""
+import math
+
+import numpy as np
+
+NFEAT = 9
+NRAD_SET = (20, 30, 50, 75)
+NRAD_MIN, NRAD_MAX = 10, 150
+SCALE_BOUNDS = (0.25, 4.0)
+TARGET_ERR = 1e-10
+_GL = {}
+
+
+def gauss_legendre(n):
+    if n not in _GL:
+        x, w = np.polynomial.legendre.leggauss(n)
+        _GL[n] = (x, w)
+    return _GL[n]
+
+
+def radial_errors(scales, expo, nrad):
+    """Relative error of the mapped Gauss-Legendre rule for int_0^inf r^2 exp(-e r^2) dr, for
+    every scale (rows) and exponent (columns)."""
+    x, w = gauss_legendre(nrad)
+    a = np.asarray(scales, dtype=np.float64)[:, None]
+    r = a * (1.0 + x[None, :]) / (1.0 - x[None, :])                # (S, n)
+    wr = w[None, :] * 2.0 * a / (1.0 - x[None, :]) ** 2 * r * r     # (S, n)
+    e = np.asarray(expo, dtype=np.float64)
+    q = np.einsum("sn,sne->se", wr, np.exp(-np.minimum(e[None, None, :] * (r * r)[:, :, None], 700.0)))
+    exact = math.sqrt(math.pi) / 4.0 * e ** -1.5
+    return np.abs(q - exact[None, :]) / exact[None, :]
+
+
+def best_scale(expo, nrad, a_ref, span=8.0, nscan=60):
+    """The scale (within a_ref / span .. a_ref * span) minimising the mean relative error over
+    the exponents, and that error."""
+    scales = a_ref * np.exp(np.linspace(-math.log(span), math.log(span), nscan))
+    err = radial_errors(scales, expo, nrad).mean(axis=1)
+    k = int(np.argmin(err))
+    return float(scales[k]), float(err[k])
+
+
+def centre_pairs(an, cartes, cent, tol=0.3):
+    """For each centre, the atom pairs (A, B) with R_B - R_A at the centre (the origin: A == B)."""
+    R = np.asarray(cartes, dtype=np.float64)
+    out = []
+    for c in np.asarray(cent, dtype=np.float64):
+        if np.linalg.norm(c) < 1e-8:
+            out.append([(a, a) for a in range(len(R))])
+            continue
+        d = R[None, :, :] - R[:, None, :] - c[None, None, :]
+        A, B = np.nonzero(np.linalg.norm(d, axis=2) < tol)
+        out.append([(int(a), int(b)) for a, b in zip(A, B) if a != b])
+    return out
+
+
+def centre_exponents(basis, pairs, cap=16):
+    """Quantiles (at most `cap`) of the product exponents 2 a_i a_j / (a_i + a_j) behind a centre."""
+    al, X, R = basis["alpha"], basis["xyz"], basis["cartes"]
+    atom_of = np.argmin(np.linalg.norm(X[:, None, :] - R[None, :, :], axis=2), axis=1)
+    by_atom = [al[atom_of == a] for a in range(len(R))]
+    es = []
+    for a, b in pairs:
+        ea, eb = by_atom[a], by_atom[b]
+        if len(ea) and len(eb):
+            es.append((2.0 * ea[:, None] * eb[None, :] / (ea[:, None] + eb[None, :])).ravel())
+    if not es:
+        return np.array([1.0])
+    e = np.sort(np.concatenate(es))
+    if len(e) > cap:
+        e = e[np.round(np.linspace(0, len(e) - 1, cap)).astype(int)]
+    return e
+
+
+def features(basis, cent, Ps, alf, nrad):
+    """Per-centre features: log scale, log Ps, log(1 + |c|), log(1 + nearest other centre),
+    10/50/90 % quantiles of log exponent, log(number of atom pairs + 1), log nrad."""
+    cent = np.asarray(cent, dtype=np.float64).reshape(-1, 3)
+    pairs = centre_pairs(basis["an"], basis["cartes"], cent)
+    F, E = [], []
+    for k, c in enumerate(cent):
+        e = centre_exponents(basis, pairs[k])
+        le = np.log(e)
+        dn = np.linalg.norm(cent - c, axis=1)
+        dn = dn[dn > 1e-9]
+        F.append([math.log(alf[k]), math.log(max(Ps[k], 1e-3)), math.log1p(np.linalg.norm(c)),
+                  math.log1p(dn.min() if len(dn) else 10.0), np.quantile(le, 0.1), np.quantile(le, 0.5),
+                  np.quantile(le, 0.9), math.log1p(len(pairs[k])), math.log(nrad)])
+        E.append(e)
+    return np.asarray(F, dtype=np.float64), E
+
+
+def targets(E, alf, nrad):
+    """Per centre: log(best scale / autogrid scale) at nrad, and log of the smallest nrad whose
+    best error is below TARGET_ERR (NRAD_MAX if none is)."""
+    T = []
+    for e, a in zip(E, alf):
+        s, _ = best_scale(e, nrad, a)
+        need = NRAD_MAX
+        for n in (10, 15, 20, 25, 30, 40, 50, 60, 75, 90, 110, 130, 150):
+            if best_scale(e, n, a)[1] <= TARGET_ERR:
+                need = n
+                break
+        T.append([math.log(s / a), math.log(need)])
+    return np.asarray(T, dtype=np.float64)
+
+
+def training_set(nmol=500, seed=20261207, nrad_set=NRAD_SET):
+    """Features and targets from autogrid's centres for nmol seeded geometries of 2-20 atoms."""
+    from . import centercalc
+    from . import workloads as W
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    for _ in range(nmol):
+        natoms = int(rng.integers(2, 21))
+        b = W.random_molecule(rng, natoms, int(rng.integers(2 * natoms, 8 * natoms + 1)))
+        cent, Ps, alf = centercalc(b["an"], b["cartes"])
+        for nrad in nrad_set:
+            F, E = features(b, cent, Ps, alf, nrad)
+            X.append(F)
+            Y.append(targets(E, alf, nrad))
+    return np.vstack(X), np.vstack(Y)
+
+
+class LearnedGrid:
+    """Per-centre radial scales and node counts predicted by a network trained on GPU."""
+
+    def __init__(self, nhidden=32, seed=1):
+        from ._lib import MLP
+        self.net = MLP(NFEAT, nhidden, 2, seed=seed)
+        self.mu = self.sd = self.lo = self.hi = None
+        self.tmu = self.tsd = None
+
+    def fit(self, X, Y, epochs=300, batch=256, lr=3e-3, seed=7):
+        X = np.asarray(X, dtype=np.float64)
+        Y = np.asarray(Y, dtype=np.float64)
+        self.mu, self.sd = X.mean(0), X.std(0) + 1e-9
+        self.lo, self.hi = X.min(0), X.max(0)
+        self.tmu, self.tsd = Y.mean(0), Y.std(0) + 1e-9
+        Xn = ((X - self.mu) / self.sd).astype(np.float32)
+        Yn = ((Y - self.tmu) / self.tsd).astype(np.float32)
+        return self.net.train(Xn, Yn, epochs=epochs, batch=batch, lr=lr, seed=seed)
+
+    def predict_raw(self, X):
+        Xn = ((np.asarray(X, dtype=np.float64) - self.mu) / self.sd).astype(np.float32)
+        return self.net.forward(Xn).astype(np.float64) * self.tsd + self.tmu
+
+    def grid(self, basis, nrad, nohydro=True):
+        """Centres, Ps and per-centre (scale, nrad) for inca_grid_radial: autogrid's values where
+        the features leave the training range or a prediction leaves its bounds."""
+        from . import centercalc
+        cent, Ps, alf = centercalc(basis["an"], basis["cartes"], nohydro=nohydro)
+        F, _ = features(basis, cent, Ps, alf, nrad)
+        pred = self.predict_raw(F)
+        inside = np.all((F >= self.lo) & (F <= self.hi), axis=1)
+        mult = np.exp(pred[:, 0])
+        ok = inside & (mult >= SCALE_BOUNDS[0]) & (mult <= SCALE_BOUNDS[1])
+        scale = np.where(ok, alf * mult, alf)
+        nr = np.clip(np.round(np.exp(pred[:, 1])), NRAD_MIN, NRAD_MAX).astype(np.int32)
+        nr = np.where(inside, nr, nrad).astype(np.int32)
+        return cent, Ps, scale, nr, ok
+
+
+def mlp_reference(params, nin, nh, nout, X, T=None):
+    """The same network in numpy (float64): outputs, and with targets the loss and its gradient
+    in the parameter layout of inca_mlp_* (used to check the GPU kernels)."""
+    p = np.asarray(params, dtype=np.float64)
+    o = 0
+
+    def take(k):
+        nonlocal o
+        v = p[o:o + k]
+        o += k
+        return v
+    W1 = take(nh * nin).reshape(nh, nin); b1 = take(nh)
+    W2 = take(nh * nh).reshape(nh, nh); b2 = take(nh)
+    W3 = take(nout * nh).reshape(nout, nh); b3 = take(nout)
+    X = np.asarray(X, dtype=np.float64)
+    a1 = np.tanh(X @ W1.T + b1)
+    a2 = np.tanh(a1 @ W2.T + b2)
+    y = a2 @ W3.T + b3
+    if T is None:
+        return y
+    n = len(X)
+    d = y - np.asarray(T, dtype=np.float64)
+    loss = float((d * d).sum() / n)
+    dy = 2.0 * d / n
+    gW3, gb3 = dy.T @ a2, dy.sum(0)
+    d2 = (dy @ W3) * (1.0 - a2 * a2)
+    gW2, gb2 = d2.T @ a1, d2.sum(0)
+    d1 = (d2 @ W2) * (1.0 - a1 * a1)
+    gW1, gb1 = d1.T @ X, d1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
+    return y, loss, g

@@ -205,6 +205,28 @@ int inca_batch_prepare(inca_ctx* ctx, double thresh, inca_counts* counts, int64_
 int inca_batch_eval(inca_ctx* ctx, int mode, double tol, double* rintra);
 
 /* ---------------------------------------------------------------------------------------
+ * A small multilayer perceptron trained and evaluated by this library's kernels, used to
+ * predict per-centre radial-grid scales for the automatic multicentre grids
+ * (inca_parallel_gb300/learned_grid.py). No counterpart in the reference (mod_autogrid,
+ * src/mod_autogrid.f90:12-185, takes every centre's scale from Bragg-Slater radii; it stays the
+ * fallback). Network: nin -> nhidden (tanh) -> nhidden (tanh) -> nout, FP32; parameters in one
+ * array: W1[nhidden][nin], b1[nhidden], W2[nhidden][nhidden], b2[nhidden], W3[nout][nhidden],
+ * b3[nout] (row-major). Loss: mean over rows of the squared error summed over outputs; Adam.
+ * X is X[n][nin], T and Y are [n][nout] (host arrays). Deterministic for a given seed. */
+typedef struct inca_mlp inca_mlp;
+int inca_mlp_create(inca_mlp** mlp, int device, int32_t nin, int32_t nhidden, int32_t nout, uint64_t seed);
+int inca_mlp_destroy(inca_mlp* mlp);
+int inca_mlp_param_count(inca_mlp* mlp, int64_t* count);
+int inca_mlp_get_params(inca_mlp* mlp, float* params);
+int inca_mlp_set_params(inca_mlp* mlp, const float* params);
+int inca_mlp_forward(inca_mlp* mlp, int64_t n, const float* X, float* Y);
+/* loss and its gradient with respect to every parameter (grad: inca_mlp_param_count floats) */
+int inca_mlp_gradient(inca_mlp* mlp, int64_t n, const float* X, const float* T, float* loss, float* grad);
+/* epochs of minibatch Adam (rows shuffled by seed); final_loss: loss over all n rows */
+int inca_mlp_train(inca_mlp* mlp, int64_t n, const float* X, const float* T, int32_t epochs, int32_t batch,
+                   float lr, uint64_t seed, float* final_loss);
+
+/* ---------------------------------------------------------------------------------------
  * Evaluation without allocation. No counterpart in the reference (the Fortran program
  * allocates its work arrays itself); this entry point exists for callers that must not
  * allocate device memory while they run: a solver that keeps all its device memory in its
