@@ -211,3 +211,74 @@ def mlp_reference(params, nin, nh, nout, X, T=None):
     gW1, gb1 = d1.T @ X, d1.sum(0)
     g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
     return y, loss, g
+
+
+def judge(lg, cases, nrad=50, nang=302, dense=(150, 974), nohydro=True, ctx=None):
+    """Radial integrals of each case (basis, ijkl, v) on autogrid's grid and on the learned grid
+    (learned scales and node counts), both against a dense autogrid grid; returns one dict per
+    case with the relative errors and the point counts."""
+    from . import Context, centercalc
+    own = ctx is None
+    ctx = ctx or Context(0)
+    out = []
+    try:
+        for b, ijkl, v in cases:
+            ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+            ctx.set_quartets(ijkl, v)
+            ctx.prepare(1e-12)
+            cent, Ps, alf = centercalc(b["an"], b["cartes"], nohydro=nohydro)
+            nq = len(Ps)
+
+            def integral(c, P, a, nr, na):
+                _, _, ng = ctx.grid_radial(np.broadcast_to(nr, (nq,)).astype(np.int32),
+                                           np.broadcast_to(na, (nq,)).astype(np.int32), a, c, P)
+                ctx.eval(mode=0)
+                return ctx.radial_integral()[0], ng
+            ref, nref = integral(cent, Ps, alf, dense[0], dense[1])
+            auto, nauto = integral(cent, Ps, alf, nrad, nang)
+            c2, P2, a2, nr2, ok = lg.grid(b, nrad, nohydro=nohydro)
+            mine, nmine = integral(c2, P2, a2, nr2, nang)
+            out.append({"centres": nq, "predicted": int(ok.sum()), "dense": ref, "dense_points": nref,
+                        "auto_err": abs(auto - ref) / abs(ref), "auto_points": nauto,
+                        "learned_err": abs(mine - ref) / abs(ref), "learned_points": nmine})
+    finally:
+        if own:
+            ctx.close()
+    return out
+
+
+def main(argv=None):
+    """Train on autogrid's centres for 500 seeded geometries of 2-20 atoms and judge the learned
+    grids against dense grids (nrad 150, nang 974) on held-out molecules with real DM2s:
+        python -m inca_parallel_gb300.learned_grid [nmol] [out.npz]"""
+    import json
+    import sys
+    import time
+    from . import workloads as W
+    args = list(sys.argv[1:] if argv is None else argv)
+    nmol = int(args[0]) if args else 500
+    t0 = time.time()
+    X, Y = training_set(nmol=nmol)
+    t1 = time.time()
+    lg = LearnedGrid(nhidden=32, seed=1)
+    loss = lg.fit(X, Y, epochs=300)
+    t2 = time.time()
+    if len(args) > 1:
+        np.savez(args[1], params=lg.net.params(), mu=lg.mu, sd=lg.sd, lo=lg.lo, hi=lg.hi, tmu=lg.tmu, tsd=lg.tsd)
+    rng = np.random.default_rng(909)
+    cases = []
+    for _ in range(8):
+        b = W.random_molecule(rng, int(rng.integers(2, 7)), int(rng.integers(10, 36)))
+        keep = (b["tmn"].sum(1) <= 1) & (b["alpha"] <= 50.0)  # where the reference's fit is exact
+        b = {**b, "alpha": b["alpha"][keep], "tmn": b["tmn"][keep], "xyz": b["xyz"][keep]}
+        nocc = max(1, min(W.electrons(b) // 2, len(b["alpha"]) // 3))
+        D, _ = W.closed_shell_density(b, nocc, int(rng.integers(1 << 30)))
+        ijkl, v = W.folded_records(D)
+        cases.append((b, ijkl, v))
+    res = judge(lg, cases)
+    print(json.dumps({"molecules": nmol, "samples": len(X), "targets_s": t1 - t0, "train_s": t2 - t1,
+                      "train_loss": loss, "held_out": res}, indent=1))
+
+
+if __name__ == "__main__":
+    main()
