@@ -69,6 +69,7 @@ SIGNATURES = {
     "inca_mlp_gradient": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP, FP, FP]),
     "inca_mlp_train": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
                                       ctypes.c_uint64, FP]),
+    "inca_eval_graph": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_double, DP]),
     "inca_batch_clear": (ctypes.c_int, [VP]),
     "inca_batch_add_closed_shell": (ctypes.c_int, [VP, ctypes.c_int32, DP, IP, DP, DP, DP, DP, ctypes.c_int,
                                                    ctypes.c_int32, DP, DP, DP, IP, ctypes.c_int, IP]),
@@ -292,6 +293,12 @@ class Context:
     def eval(self, mode=INCA_FP64, tol=1e-10, copy=True):
         iv = np.zeros(self.ngrid) if copy else None
         self._check(self.lib.inca_eval(self.h, mode, tol, _d(iv)))
+        return iv
+
+    def eval_graph(self, mode=INCA_MIXED, tol=1e-10, copy=True):
+        """inca_eval through a captured CUDA graph (the first call per grid/records/tol captures)."""
+        iv = np.zeros(self.ngrid) if copy else None
+        self._check(self.lib.inca_eval_graph(self.h, mode, tol, _d(iv)))
         return iv
 
     def radial_integral(self):

@@ -112,6 +112,10 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_scratch_s.release();
   c->d_tiles.release();
   c->d_tiles_s.release();
+  c->d_exptab.release();
+  c->d_pmol.release();
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->graph_exec = nullptr;
   cudaStreamDestroy(c->stream);
   delete c;
   return INCA_OK;
@@ -344,6 +348,14 @@ int inca_grid_copy(inca_ctx* c, double* r, double* w, double* wvee, int32_t* cma
 int inca_eval(inca_ctx* c, int mode, double tol, double* ivec) {
   CTX_CHECK(c);
   const int st = eval_device(c, mode, tol);
+  if (st) return st;
+  if (ivec) INCA_CUDA(c, cudaMemcpy(ivec, c->d_ivec.p, sizeof(double) * c->ngrid, cudaMemcpyDeviceToHost));
+  return INCA_OK;
+}
+
+int inca_eval_graph(inca_ctx* c, int mode, double tol, double* ivec) {
+  CTX_CHECK(c);
+  const int st = eval_device(c, mode, tol, true);
   if (st) return st;
   if (ivec) INCA_CUDA(c, cudaMemcpy(ivec, c->d_ivec.p, sizeof(double) * c->ngrid, cudaMemcpyDeviceToHost));
   return INCA_OK;

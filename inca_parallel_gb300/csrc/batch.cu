@@ -21,7 +21,6 @@
 namespace inca {
 
 int prepare_device(inca_ctx* c, double thresh, int normalize);
-int eval_device(inca_ctx* c, int mode, double tol);
 int radial_plot_device(inca_ctx* c, double* rintra);
 
 namespace {

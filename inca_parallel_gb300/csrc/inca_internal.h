@@ -205,6 +205,15 @@ struct inca_ctx {
   int t_kernel_launches = 0, t_launches = 0;
   int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0, corrected_points = 0;
   int64_t launches = 0;  // own kernel launches since creation
+
+  // graph replay of the mixed evaluation (captured for one grid, set of records and tolerance)
+  inca::DevBuf<float2> d_exptab;  // 2^(j/256) table of the double-float exp2
+  int64_t prepare_count = 0;      // bumped by every inca_prepare / batch preparation
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_grid = -1, graph_prep = -1, graph_launches = 0;
+  double graph_eps = 0.0;
+  bool graph_fused = false, graph_drop = false;
+  const void* graph_bufs[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 // ---- internal entry points between translation units
@@ -221,7 +230,7 @@ int64_t closed_shell_records(int n, int unique);
 int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int base, int64_t at);
 
 // intracule_eval.cu
-int eval_device(inca_ctx* c, int mode, double tol);
+int eval_device(inca_ctx* c, int mode, double tol, bool graph = false);
 
 // grid_build.cu
 int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,

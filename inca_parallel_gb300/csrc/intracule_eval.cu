@@ -16,7 +16,8 @@
 
 namespace inca {
 
-int eval_mixed(inca_ctx* c, double tol);  // mixed_eval.cu
+int eval_mixed(inca_ctx* c, double tol);        // mixed_eval.cu
+int eval_mixed_graph(inca_ctx* c, double tol);  // mixed_eval.cu
 
 namespace {
 
@@ -98,7 +99,7 @@ int choose_splits(int64_t tiles, int64_t nchunks, int num_sms, int ctas_per_sm) 
   return static_cast<int>(s);
 }
 
-int eval_device(inca_ctx* c, int mode, double tol) {
+int eval_device(inca_ctx* c, int mode, double tol, bool graph) {
   if (!c->prepared) return set_error(c, INCA_E_STATE, "inca_eval: call inca_prepare first");
   if (c->grid_kind == GRID_NONE || c->ngrid <= 0) return set_error(c, INCA_E_STATE, "inca_eval: no grid");
   if (c->batch_molecules > 0 && c->batch_grid_version != c->grid_version)
@@ -108,7 +109,7 @@ int eval_device(inca_ctx* c, int mode, double tol) {
   c->t_kernel_launches = c->t_launches = 0;
   c->pairs_fp32 = c->pairs_fp64 = c->pairs_skip = c->corrected_points = 0;
   if (mode == INCA_MIXED) {
-    const int st = eval_mixed(c, tol > 0 ? tol : 1e-10);
+    const int st = graph ? eval_mixed_graph(c, tol > 0 ? tol : 1e-10) : eval_mixed(c, tol > 0 ? tol : 1e-10);
     if (st == INCA_OK) c->evaluated = true;
     return st;
   }

@@ -1163,6 +1163,69 @@ __global__ void k_sum_drop(int64_t ntiles, const MolWork* __restrict__ mw, int n
   out[t] = s;
 }
 
+// ---- thresholds of the outputs, on the device (no host round trip between the passes)
+// The threshold of an output: 3 sigma of the uncorrected rounding errors within the absolute
+// budget B (tolerance times a lower bound of |O|, less the left-out bound mass):
+// T = tscale B^2 / E_O.
+__device__ __forceinline__ double tau_budget(double B, double M, double tscale) {
+  return M > 0.0 ? tscale * B * B / M : HUGE_VAL;
+}
+__device__ __forceinline__ double ull_to_double(unsigned long long u) { return __longlong_as_double(static_cast<long long>(u)); }
+
+// Estimates, segments of a radial or scan grid: the sampled sums sam[3s..3s+2] = (sum w I~,
+// sum w E~, sum w) over the sampled points of segment s, all[3s+2] = sum w over all its points.
+__global__ void k_thr_est_seg(int nseg, const double* __restrict__ sam, const double* __restrict__ all,
+                              const int64_t* __restrict__ off, double eps, double tscale, double safety,
+                              double drop_half, double nq, double* T, double* Theta) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const double wsam = sam[3 * s + 2], wtot = all[3 * s + 2];
+  const double f = wsam > 0.0 ? wtot / wsam : 0.0;
+  const double O = sam[3 * s] * f, M = sam[3 * s + 1] * f;
+  const double lo = fmax(fabs(O) - M, 0.0);
+  T[s] = (wsam > 0.0 && M > 0.0) ? safety * tau_budget(eps * lo, M, tscale) : 0.0;
+  // drop threshold per point: theta_g = Theta / w_g with sum_g w_g nq theta_g at most
+  // drop_frac eps |O| (half of it here, for the sampling error of the estimate)
+  const double npts = static_cast<double>(off[s + 1] - off[s]);
+  Theta[s] = wsam > 0.0 ? drop_half * eps * lo / (nq * fmax(npts, 1.0)) : 0.0;
+}
+
+// Estimates, cube (max-norm): from the sampled max |I~| and max E~.
+__global__ void k_thr_est_max(const unsigned long long* __restrict__ mx, double eps, double tscale, double safety,
+                              double margin, double drop_half, double nq, double* T, double* Theta) {
+  if (threadIdx.x + blockIdx.x != 0) return;
+  const double imax = ull_to_double(mx[0]), emax = ull_to_double(mx[1]);
+  const double x = eps * imax;
+  T[0] = emax > 0.0 ? safety * tscale * x * x / (margin * emax) : 0.0;
+  Theta[0] = drop_half * eps * imax / nq;
+}
+
+// Exact thresholds, segments: sums ex[3s..] = (sum w I~, sum w E~, .) over all points and, with
+// dropping, dd[3s] = sum w D (bound mass left out); *retry set when D took more than half the
+// budget (the pass is then repeated without dropping).
+__global__ void k_thr_exact_seg(int nseg, const double* __restrict__ ex, const double* __restrict__ dd, int use_drop,
+                                double eps, double tscale, double* T, int* retry) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const double D = use_drop ? dd[3 * s] : 0.0;
+  const double lo = fmax(fabs(ex[3 * s]) - ex[3 * s + 1] - D, 0.0);
+  const double B = eps * lo - D;
+  if (use_drop && B < 0.5 * eps * lo) atomicExch(retry, 1);
+  T[s] = tau_budget(fmax(B, 0.0), ex[3 * s + 1], tscale);
+}
+
+// Exact threshold, cube: from max |I~| and the largest left-out mass of a tile.
+__global__ void k_thr_exact_max(const unsigned long long* __restrict__ mx, const unsigned long long* __restrict__ mdrop,
+                                int use_drop, double eps, double tscale, double* T, int* retry) {
+  if (threadIdx.x + blockIdx.x != 0) return;
+  const double imax = ull_to_double(mx[0]);
+  const double dmx = use_drop ? ull_to_double(mdrop[0]) : 0.0;
+  const double B = eps * imax - dmx;
+  if (use_drop && B < 0.5 * eps * imax) atomicExch(retry, 1);
+  const double b = fmax(B, 0.0);
+  T[0] = tscale * b * b;
+}
+
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
@@ -1327,326 +1390,281 @@ unsigned persistent_ctas(int64_t nitems, int num_sms) {
 
 }  // namespace
 
-int eval_mixed(inca_ctx* c, double eps) {
-  const int64_t ngrid = c->ngrid;
-  const int nchunks = static_cast<int>(c->chunks.size());
-  if (nchunks == 0) {
-    INCA_CUDA(c, cudaMemsetAsync(c->d_ivec.p, 0, sizeof(double) * ngrid, c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    return INCA_OK;
-  }
-  const int64_t launches0 = c->launches;
-  const bool fused =
-      (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN || c->grid_kind == GRID_CUBE) && ngrid >= kFuseMinPoints;
-  Events ev;
-  for (auto& e : ev.e) INCA_CUDA(c, cudaEventCreate(&e));
-  INCA_CUDA(c, cudaEventRecord(ev.e[0], c->stream));
-  int st = prepare_sorted_grid(c, fused);
-  if (st) return st;
-  const int64_t nwt = c->ntiles;
-  const int64_t ngroups = nwt * kPPT;
-  int64_t nitems = 0, npart = 0, ndrop = 0;
-  const std::vector<MolWork> hmw = work_table(c->mol_span, c->mol_chunks, c->num_sms, &nitems, &npart, &ndrop);
-  const int nmol = static_cast<int>(hmw.size());
-  const unsigned nctas = persistent_ctas(nitems, c->num_sms);
-  const float* wbox = c->d_wtbox.p;
-  const float* gbox = c->d_wtbox.p + 8 * nwt;
-  const TileInfo* tiles = c->d_tiles.p;
+namespace {
 
+double env_knob(const char* name, double dflt, double lo, double hi) {
+  if (const char* env = std::getenv(name)) {
+    char* end = nullptr;
+    const double v = std::strtod(env, &end);
+    if (end != env && std::isfinite(v) && v >= lo && v < hi) return v;
+  }
+  return dflt;
+}
+
+// Everything an evaluation needs that the host decides: sizes, knobs, buffers (carved from the
+// context's scratch) and uploaded tables. The launch sequence then runs on the device alone.
+struct MixedPlan {
+  bool fused = false;
+  int mode = 2, nseg = 1, emode = 0, nmol = 1;
+  const int* seg_of = nullptr;
+  int64_t ngrid = 0, nwt = 0, ngroups = 0, nitems = 0, npart = 0, ndrop = 0;
+  int64_t ns = 0, nitems_s = 0, npart_s = 0;
+  unsigned nctas = 1, nctas_s = 1, gblk = 1, tblk = 1;
+  int stage_floats = 0;
+  size_t dsmem = 0;
+  double eps = 0, tau_scale = 0, safety = 0, drop_frac = 0, nq = 1;
+  double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dsam, *dall, *dex, *ddrop, *dTest, *dTheta, *dT, *dmass, *Dt, *Dpt;
+  double *q1 = nullptr, *qabs = nullptr, *Iss = nullptr, *Mss = nullptr, *Ios = nullptr, *Mos = nullptr, *ws = nullptr;
+  float *glt, *ptau, *ptau_est, *ptheta, *ltdrop;
+  unsigned long long *stats, *dmax, *dmax2, *work;
+  MolWork *mwdev, *mws = nullptr;
+  int *errw, *retry;
+  int64_t* doff;
+  const float2* tab;
+};
+
+int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
+  P.ngrid = c->ngrid;
+  const int64_t ngrid = P.ngrid;
+  P.fused = (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN || c->grid_kind == GRID_CUBE) &&
+            ngrid >= kFuseMinPoints;
+  int st = prepare_sorted_grid(c, P.fused);
+  if (st) return st;
+  P.eps = eps;
+  // knobs (environment, read per evaluation; tuning and test aids)
+  P.tau_scale = env_knob("INCA_TAU_SCALE", kTauScale, 1e-300, HUGE_VAL);
+  P.drop_frac = env_knob("INCA_DROP_FRACTION", kDropFrac, 0.0, 0.5);
+  P.safety = env_knob("INCA_EST_SAFETY", kEstSafety, 0.0, HUGE_VAL);
+  P.nwt = c->ntiles;
+  P.ngroups = P.nwt * kPPT;
+  const std::vector<MolWork> hmw = work_table(c->mol_span, c->mol_chunks, c->num_sms, &P.nitems, &P.npart, &P.ndrop);
+  P.nmol = static_cast<int>(hmw.size());
+  P.nctas = persistent_ctas(P.nitems, c->num_sms);
+  std::vector<MolWork> hmw_s;
+  if (P.fused) {
+    P.ns = c->nsample;
+    int64_t ndrop_s = 0;
+    hmw_s = work_table(c->mol_span_s, c->mol_chunks, c->num_sms, &P.nitems_s, &P.npart_s, &ndrop_s);
+    P.nctas_s = persistent_ctas(P.nitems_s, c->num_sms);
+  }
+  // survivors of the largest molecule: an upper bound on the terms left out at a point
+  P.nq = static_cast<double>(std::max<int64_t>(*std::max_element(c->mol_surv.begin(), c->mol_surv.end()), 1));
   // outputs and their segments: radial grid (one integral), scan grid (one I(s) per shell),
   // cube (max-norm), explicit points (each point)
-  int mode = 2;
   std::vector<int64_t> off;
-  const int* seg_of = nullptr;
   if (c->grid_kind == GRID_RADIAL) {
-    mode = 0;
+    P.mode = 0;
     off = {0, ngrid};
   } else if (c->grid_kind == GRID_SCAN) {
-    mode = 0;
+    P.mode = 0;
     off.assign(c->nradi + 1, 0);
     for (int s = 0; s < c->nradi; ++s) off[s + 1] = off[s] + c->h_smn[s];
-    seg_of = c->d_cmap.p;  // shell of each scan point
+    P.seg_of = c->d_cmap.p;  // shell of each scan point
   } else if (c->grid_kind == GRID_CUBE) {
-    mode = 1;
+    P.mode = 1;
   }
-  const int nseg = off.empty() ? 1 : static_cast<int>(off.size()) - 1;
-
-  // scratch: pass sums and error-bound sums (per molecule: splits x points), I~ / E~ sorted and grid order,
-  // thresholds, left-out bound mass per tile, statistics, the exp table, segment sums
-  double *p1, *pabs, *p2, *Is, *Ms, *Io, *Mo, *dout, *dT, *dmass, *Dt, *Dpt;
-  float *glt, *ptau, *ptau_est, *ptheta, *ltdrop;
-  unsigned long long *stats, *dmax, *work;
-  MolWork* mwdev;
-  int* errw;
-  int64_t* doff;
-  float2* tab;
+  P.emode = P.mode == 0 ? 0 : 3;
+  P.nseg = off.empty() ? 1 : static_cast<int>(off.size()) - 1;
+  const int nseg = P.nseg;
   auto layout = [&](Carve& cv) {
-    p1 = cv.take<double>(npart);
-    pabs = cv.take<double>(npart);
-    p2 = cv.take<double>(npart);
-    Is = cv.take<double>(ngrid);
-    Ms = cv.take<double>(ngrid);
-    Io = cv.take<double>(ngrid);
-    Mo = cv.take<double>(ngrid);
-    glt = cv.take<float>(ngroups);
-    ptau = cv.take<float>(ngrid);
-    ptau_est = cv.take<float>(fused ? ngrid : 1);
-    ptheta = cv.take<float>(fused ? ngrid : 1);
-    ltdrop = cv.take<float>(fused ? nwt : 1);
-    dmass = cv.take<double>(fused ? ndrop : 1);
-    Dt = cv.take<double>(fused ? nwt : 1);
-    Dpt = cv.take<double>(fused ? ngrid : 1);
-    stats = cv.take<unsigned long long>(16);
-    work = cv.take<unsigned long long>(4);
-    mwdev = cv.take<MolWork>(nmol);
-    dmax = cv.take<unsigned long long>(2);
-    errw = cv.take<int>(4);
-    tab = cv.take<float2>(kExpTab + 1);
-    dout = cv.take<double>(6 * nseg);
-    dT = cv.take<double>(nseg);
-    doff = cv.take<int64_t>(nseg + 1);
+    P.p1 = cv.take<double>(P.npart);
+    P.pabs = cv.take<double>(P.npart);
+    P.p2 = cv.take<double>(P.npart);
+    P.Is = cv.take<double>(ngrid);
+    P.Ms = cv.take<double>(ngrid);
+    P.Io = cv.take<double>(ngrid);
+    P.Mo = cv.take<double>(ngrid);
+    P.glt = cv.take<float>(P.ngroups);
+    P.ptau = cv.take<float>(ngrid);
+    P.ptau_est = cv.take<float>(P.fused ? ngrid : 1);
+    P.ptheta = cv.take<float>(P.fused ? ngrid : 1);
+    P.ltdrop = cv.take<float>(P.fused ? P.nwt : 1);
+    P.dmass = cv.take<double>(P.fused ? P.ndrop : 1);
+    P.Dt = cv.take<double>(P.fused ? P.nwt : 1);
+    P.Dpt = cv.take<double>(P.fused ? ngrid : 1);
+    P.stats = cv.take<unsigned long long>(16);
+    P.work = cv.take<unsigned long long>(4);
+    P.mwdev = cv.take<MolWork>(P.nmol);
+    P.mws = cv.take<MolWork>(P.nmol);
+    P.dmax = cv.take<unsigned long long>(2);
+    P.dmax2 = cv.take<unsigned long long>(2);
+    P.errw = cv.take<int>(4);
+    P.retry = cv.take<int>(4);
+    P.dsam = cv.take<double>(3 * nseg);
+    P.dall = cv.take<double>(3 * nseg);
+    P.dex = cv.take<double>(3 * nseg);
+    P.ddrop = cv.take<double>(3 * nseg);
+    P.dTest = cv.take<double>(nseg);
+    P.dTheta = cv.take<double>(nseg);
+    P.dT = cv.take<double>(nseg);
+    P.doff = cv.take<int64_t>(nseg + 1);
   };
   Carve dry{nullptr};
   layout(dry);
   if (c->d_scratch.reserve(dry.off + 256)) return set_error(c, INCA_E_NOMEM, "mixed scratch");
   Carve cv{c->d_scratch.p};
   layout(cv);
-  // INCA_TAU_SCALE overrides the variance factor of the thresholds (tuning and test knob)
-  double tau_scale = kTauScale;
-  if (const char* env = std::getenv("INCA_TAU_SCALE")) {
-    char* end = nullptr;
-    const double v = std::strtod(env, &end);
-    if (end != env && v > 0.0 && std::isfinite(v)) tau_scale = v;
-  }
-  // INCA_DROP_FRACTION overrides the share of the tolerance given to left-out terms (0: none)
-  double drop_frac = kDropFrac;
-  if (const char* env = std::getenv("INCA_DROP_FRACTION")) {
-    char* end = nullptr;
-    const double v = std::strtod(env, &end);
-    if (end != env && v >= 0.0 && v < 0.5) drop_frac = v;
-  }
-  const std::vector<float2> htab = exp2_table();
-  INCA_CUDA(c, cudaMemcpyAsync(tab, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice, c->stream));
-  INCA_CUDA(c, cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), c->stream));
-  INCA_CUDA(c, cudaMemsetAsync(work, 0, 4 * sizeof(unsigned long long), c->stream));
-  INCA_CUDA(c, cudaMemcpyAsync(mwdev, hmw.data(), sizeof(MolWork) * nmol, cudaMemcpyHostToDevice, c->stream));
-  INCA_CUDA(c, cudaMemsetAsync(errw, 0, 4 * sizeof(int), c->stream));
-  if (!off.empty())
-    INCA_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
-  int max_stride = 4;
-  for (const ClassSeg& sg : c->classes) max_stride = std::max(max_stride, sg.stride32);
-  if (max_stride > kMaxStride32) return set_error(c, INCA_E_LIMIT, "inca_eval: record stride above the maximum");
-  const int stage_floats = kChunkMax * max_stride;
-  const size_t dsmem = 128 + 2 * sizeof(float) * stage_floats;
-  const unsigned gblk = static_cast<unsigned>((ngroups + 7) / 8);
-  const unsigned tblk = static_cast<unsigned>((nwt + 7) / 8);
-  std::vector<double> hseg(6 * nseg), segT(nseg), segD(nseg, 0.0);
-
-  // segment sums of w I~, w E~, w (first three) and, with a second weight array, w2 (sixth)
-  auto seg_sums = [&](const double* w, const double* I, const double* M, const double* w2) -> int {
-    INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, w, I, M, dout);
-    if (w2) INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, w2, I, M, dout + 3 * nseg);
-    INCA_CUDA(c, cudaMemcpyAsync(hseg.data(), dout, sizeof(double) * (w2 ? 6 : 3) * nseg, cudaMemcpyDeviceToHost,
-                                 c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    return INCA_OK;
-  };
-  auto absmax = [&](const double* I, const double* M, int64_t n, double* imax, double* emax) -> int {
-    INCA_CUDA(c, cudaMemsetAsync(dmax, 0, 2 * sizeof(unsigned long long), c->stream));
-    const unsigned nb = static_cast<unsigned>(std::min<int64_t>(nblk(n), 4096));
-    INCA_LAUNCH(c, k_absmax2, nb, 256, 0, n, I, M, dmax);
-    unsigned long long hm[2] = {0, 0};
-    INCA_CUDA(c, cudaMemcpyAsync(hm, dmax, sizeof(hm), cudaMemcpyDeviceToHost, c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    std::memcpy(imax, &hm[0], sizeof(double));
-    std::memcpy(emax, &hm[1], sizeof(double));
-    return INCA_OK;
-  };
-  // threshold of an output: 3 sigma of the uncorrected rounding errors within the absolute
-  // budget B (tolerance times a lower bound of |O|, less the left-out bound mass)
-  auto tau_of_budget = [&](double B, double M) { return M > 0.0 ? tau_scale * B * B / M : HUGE_VAL; };
-
-  // ---- estimates from the grid sample (one-pass form): thresholds and drop thresholds
-  bool use_drop = false;
-  if (fused) {
-    // INCA_EST_SAFETY overrides the factor applied to the estimated thresholds (a test and
-    // tuning knob: larger values trade correction-pass work for one-pass work)
-    double safety = kEstSafety;
-    if (const char* env = std::getenv("INCA_EST_SAFETY")) {
-      char* end = nullptr;
-      const double v = std::strtod(env, &end);
-      if (end != env && v >= 0.0 && std::isfinite(v)) safety = v;
-    }
-    const int64_t ns = c->nsample;
-    int64_t nitems_s = 0, npart_s = 0, ndrop_s = 0;
-    const std::vector<MolWork> hmw_s =
-        work_table(c->mol_span_s, c->mol_chunks, c->num_sms, &nitems_s, &npart_s, &ndrop_s);
-    double *q1, *qabs, *Iss, *Mss, *Ios, *Mos, *ws;
-    MolWork* mws;
+  if (P.fused) {
     auto layout_s = [&](Carve& cs) {
-      q1 = cs.take<double>(npart_s);
-      qabs = cs.take<double>(npart_s);
-      mws = cs.take<MolWork>(nmol);
-      Iss = cs.take<double>(ns);
-      Mss = cs.take<double>(ns);
-      Ios = cs.take<double>(ngrid);
-      Mos = cs.take<double>(ngrid);
-      ws = cs.take<double>(ngrid);
+      P.q1 = cs.take<double>(P.npart_s);
+      P.qabs = cs.take<double>(P.npart_s);
+      P.Iss = cs.take<double>(P.ns);
+      P.Mss = cs.take<double>(P.ns);
+      P.Ios = cs.take<double>(ngrid);
+      P.Mos = cs.take<double>(ngrid);
+      P.ws = cs.take<double>(ngrid);
     };
     Carve dry_s{nullptr};
     layout_s(dry_s);
     if (c->d_scratch_s.reserve(dry_s.off + 256)) return set_error(c, INCA_E_NOMEM, "sample scratch");
     Carve cs{c->d_scratch_s.p};
     layout_s(cs);
-    INCA_CUDA(c, cudaMemcpyAsync(mws, hmw_s.data(), sizeof(MolWork) * nmol, cudaMemcpyHostToDevice, c->stream));
-    INCA_LAUNCH(c, k_pass1<false>, persistent_ctas(nitems_s, c->num_sms), 32, dsmem, c->d_chunks.p, mws, nmol,
-                c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, nitems_s,
-                stage_floats, nullptr, nullptr, nullptr, q1, qabs, nullptr, work + 3, stats + 8, errw);
-    INCA_CUDA(c, cudaGetLastError());
-    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, mws, nmol, q1, nullptr, Iss);
-    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, mws, nmol, qabs, nullptr, Mss);
-    std::vector<double> segTheta(nseg, 0.0);
-    // survivors of the largest molecule: an upper bound on the terms left out at a point
-    const double nq = static_cast<double>(
-        std::max<int64_t>(*std::max_element(c->mol_surv.begin(), c->mol_surv.end()), 1));
-    int emode = 0;
-    if (mode == 0) {
-      INCA_CUDA(c, cudaMemsetAsync(Ios, 0, sizeof(double) * ngrid, c->stream));
-      INCA_CUDA(c, cudaMemsetAsync(Mos, 0, sizeof(double) * ngrid, c->stream));
-      INCA_CUDA(c, cudaMemsetAsync(ws, 0, sizeof(double) * ngrid, c->stream));
-      INCA_LAUNCH(c, k_scatter_sample, nblk(ns), 256, 0, ns, c->d_perm_s.p, Iss, Mss, c->d_w.p, Ios, Mos, ws);
-      if ((st = seg_sums(ws, Ios, Mos, c->d_w.p))) return st;
-      for (int s = 0; s < nseg; ++s) {
-        const double wsam = hseg[3 * s + 2], wtot = hseg[3 * nseg + 3 * s + 2];
-        const double f = wsam > 0.0 ? wtot / wsam : 0.0;
-        const double O = hseg[3 * s] * f, M = hseg[3 * s + 1] * f;
-        const double lo = std::max(std::fabs(O) - M, 0.0);
-        segT[s] = (wsam > 0.0 && M > 0.0) ? safety * tau_of_budget(eps * lo, M) : 0.0;
-        // drop threshold per point: theta_g = Theta / w_g with sum_g w_g nq theta_g equal to
-        // drop_frac eps |O| (half the estimate, for its sampling error)
-        const double npts = static_cast<double>(off[s + 1] - off[s]);
-        segTheta[s] = wsam > 0.0 ? 0.5 * drop_frac * eps * lo / (nq * std::max(npts, 1.0)) : 0.0;
-      }
-    } else {
-      emode = 3;
-      double imax = 0.0, emax = 0.0;
-      if ((st = absmax(Iss, Mss, ns, &imax, &emax))) return st;
-      segT[0] = emax > 0.0 ? safety * tau_of_budget(eps * imax, kCubeMargin * emax) : 0.0;
-      segTheta[0] = 0.5 * drop_frac * eps * imax / nq;
-    }
-    INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-    INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
-                nullptr, eps, tau_scale, nullptr, ptau_est);
-    use_drop = drop_frac > 0.0;
-    if (use_drop) {
-      // (pageable host copies are staged before the call returns; the stream orders the rest)
-      INCA_CUDA(c, cudaMemcpyAsync(dT, segTheta.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-      INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, emode, c->d_perm.p, seg_of, dT, c->d_w.p, nullptr,
-                  nullptr, eps, tau_scale, nullptr, ptheta);
-      INCA_LAUNCH(c, k_tile_min_log2, tblk, 256, 0, tiles, nwt, ptheta, ltdrop);
-    }
-    INCA_CUDA(c, cudaGetLastError());
   }
+  if (c->d_exptab.n == 0) {
+    if (c->d_exptab.reserve(kExpTab + 1)) return set_error(c, INCA_E_NOMEM, "exp table");
+    const std::vector<float2> htab = exp2_table();
+    INCA_CUDA(c, cudaMemcpy(c->d_exptab.p, htab.data(), sizeof(float2) * htab.size(), cudaMemcpyHostToDevice));
+  }
+  P.tab = c->d_exptab.p;
+  INCA_CUDA(c, cudaMemcpyAsync(P.mwdev, hmw.data(), sizeof(MolWork) * P.nmol, cudaMemcpyHostToDevice, c->stream));
+  if (P.fused)
+    INCA_CUDA(c, cudaMemcpyAsync(P.mws, hmw_s.data(), sizeof(MolWork) * P.nmol, cudaMemcpyHostToDevice, c->stream));
+  if (!off.empty())
+    INCA_CUDA(c, cudaMemcpyAsync(P.doff, off.data(), sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, c->stream));
+  INCA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host tables above are stack-owned
+  int max_stride = 4;
+  for (const ClassSeg& sg : c->classes) max_stride = std::max(max_stride, sg.stride32);
+  if (max_stride > kMaxStride32) return set_error(c, INCA_E_LIMIT, "inca_eval: record stride above the maximum");
+  P.stage_floats = kChunkMax * max_stride;
+  P.dsmem = 128 + 2 * sizeof(float) * P.stage_floats;
+  P.gblk = static_cast<unsigned>((P.ngroups + 7) / 8);
+  P.tblk = static_cast<unsigned>((P.nwt + 7) / 8);
+  return INCA_OK;
+}
 
-  bool run_pass2 = true;
-  for (int attempt = 0;; ++attempt) {
-    // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
-    // terms below the drop thresholds left out)
-    INCA_CUDA(c, cudaEventRecord(ev.e[1], c->stream));
-    if (fused)
-      INCA_LAUNCH(c, k_pass1<true>, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p,
-                  c->d_phi.p, c->d_plo.p, tiles, wbox, nitems, stage_floats, ptau_est, tab,
-                  use_drop ? ltdrop : nullptr, p1, pabs, dmass, work, stats, errw);
-    else
-      INCA_LAUNCH(c, k_pass1<false>, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p,
-                  c->d_phi.p, c->d_plo.p, tiles, wbox, nitems, stage_floats, nullptr, nullptr, nullptr, p1, pabs,
-                  nullptr, work, stats, errw);
-    INCA_CUDA(c, cudaGetLastError());
-    INCA_CUDA(c, cudaEventRecord(ev.e[2], c->stream));
-    INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, p1, nullptr, Is);
-    INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, pabs, nullptr, Ms);
-    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, Io);
-    if (use_drop) {
-      INCA_LAUNCH(c, k_sum_drop, nblk(nwt), 256, 0, nwt, mwdev, nmol, dmass, Dt);
-      INCA_LAUNCH(c, k_tile_to_points, tblk, 256, 0, tiles, nwt, c->d_perm.p, Dt, Dpt);
-    }
-
-    // ---- exact thresholds of the outputs
-    bool retry = false;
-    if (mode == 0) {
-      INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Ms, Mo);
-      if (use_drop) {  // sum_g w_g D_g per segment (first of the three sums k_seg_sums writes)
-        INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, doff, c->d_w.p, Dpt, Dpt, dout + 3 * nseg);
-        INCA_CUDA(c, cudaMemcpyAsync(hseg.data() + 3 * nseg, dout + 3 * nseg, sizeof(double) * 3 * nseg,
-                                     cudaMemcpyDeviceToHost, c->stream));
-        INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-        for (int s = 0; s < nseg; ++s) segD[s] = hseg[3 * nseg + 3 * s];
-      }
-      if ((st = seg_sums(c->d_w.p, Io, Mo, nullptr))) return st;
-      for (int s = 0; s < nseg; ++s) {
-        const double D = use_drop ? segD[s] : 0.0;
-        const double lo = std::max(std::fabs(hseg[3 * s]) - hseg[3 * s + 1] - D, 0.0);
-        const double B = eps * lo - D;
-        if (use_drop && B < 0.5 * eps * lo) retry = true;
-        segT[s] = tau_of_budget(std::max(B, 0.0), hseg[3 * s + 1]);
-      }
-    } else if (mode == 1) {
-      double imax = 0.0, emax = 0.0, dmx = 0.0, unused = 0.0;
-      if ((st = absmax(Is, Ms, ngrid, &imax, &emax))) return st;
-      if (use_drop && (st = absmax(Dt, Dt, nwt, &dmx, &unused))) return st;
-      const double B = eps * imax - dmx;
-      if (use_drop && B < 0.5 * eps * imax) retry = true;
-      segT[0] = tau_scale * std::max(B, 0.0) * std::max(B, 0.0);
+// The device work of one evaluation (no host synchronisation: it can be captured in a graph).
+// ev (optional) gets events around the pass over all terms and the correction pass.
+int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
+  const int64_t ngrid = P.ngrid, nwt = P.nwt;
+  const int nseg = P.nseg;
+  const TileInfo* tiles = c->d_tiles.p;
+  const float* wbox = c->d_wtbox.p;
+  const float* gbox = c->d_wtbox.p + 8 * nwt;
+  INCA_CUDA(c, cudaMemsetAsync(P.stats, 0, 16 * sizeof(unsigned long long), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(P.work, 0, 4 * sizeof(unsigned long long), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(P.errw, 0, 4 * sizeof(int), c->stream));
+  INCA_CUDA(c, cudaMemsetAsync(P.retry, 0, 4 * sizeof(int), c->stream));
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[0], c->stream));
+  const unsigned sblk = static_cast<unsigned>((nseg + 127) / 128);
+  // ---- estimates from the grid sample (one-pass form): thresholds and drop thresholds
+  if (P.fused) {
+    const int64_t ns = P.ns;
+    INCA_LAUNCH(c, k_pass1<false>, P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p, c->d_rec32.p,
+                c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, P.nitems_s, P.stage_floats, nullptr,
+                nullptr, nullptr, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
+    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, P.mws, P.nmol, P.qabs, nullptr, P.Mss);
+    if (P.mode == 0) {
+      INCA_CUDA(c, cudaMemsetAsync(P.Ios, 0, sizeof(double) * ngrid, c->stream));
+      INCA_CUDA(c, cudaMemsetAsync(P.Mos, 0, sizeof(double) * ngrid, c->stream));
+      INCA_CUDA(c, cudaMemsetAsync(P.ws, 0, sizeof(double) * ngrid, c->stream));
+      INCA_LAUNCH(c, k_scatter_sample, nblk(ns), 256, 0, ns, c->d_perm_s.p, P.Iss, P.Mss, c->d_w.p, P.Ios, P.Mos, P.ws);
+      INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, P.doff, P.ws, P.Ios, P.Mos, P.dsam);
+      INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, P.doff, c->d_w.p, P.Ios, P.Mos, P.dall);
+      INCA_LAUNCH(c, k_thr_est_seg, sblk, 128, 0, nseg, P.dsam, P.dall, P.doff, P.eps, P.tau_scale, P.safety,
+                  0.5 * P.drop_frac, P.nq, P.dTest, P.dTheta);
     } else {
-      segT[0] = 0.0;
+      INCA_CUDA(c, cudaMemsetAsync(P.dmax, 0, 2 * sizeof(unsigned long long), c->stream));
+      INCA_LAUNCH(c, k_absmax2, static_cast<unsigned>(std::min<int64_t>(nblk(ns), 4096)), 256, 0, ns, P.Iss, P.Mss,
+                  P.dmax);
+      INCA_LAUNCH(c, k_thr_est_max, 1, 32, 0, P.dmax, P.eps, P.tau_scale, P.safety, kCubeMargin, 0.5 * P.drop_frac,
+                  P.nq, P.dTest, P.dTheta);
     }
-    if (retry && attempt == 0) {  // too much was left out: once more without leaving terms out
-      use_drop = false;
-      INCA_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), c->stream));
-      INCA_CUDA(c, cudaMemsetAsync(work, 0, sizeof(unsigned long long), c->stream));
-      continue;
+    INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTest, c->d_w.p,
+                nullptr, nullptr, P.eps, P.tau_scale, nullptr, P.ptau_est);
+    if (use_drop) {
+      INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTheta,
+                  c->d_w.p, nullptr, nullptr, P.eps, P.tau_scale, nullptr, P.ptheta);
+      INCA_LAUNCH(c, k_tile_min_log2, P.tblk, 256, 0, tiles, nwt, P.ptheta, P.ltdrop);
     }
-    break;
   }
-  INCA_CUDA(c, cudaMemcpyAsync(dT, segT.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, c->stream));
-  INCA_LAUNCH(c, k_thresholds, gblk, 256, 0, tiles, ngroups, mode, c->d_perm.p, seg_of, dT, c->d_w.p, Is, Ms, eps,
-              tau_scale, fused ? nullptr : glt, ptau);
+  // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
+  // terms below the drop thresholds left out)
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[1], c->stream));
+  if (P.fused)
+    INCA_LAUNCH(c, k_pass1<true>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+                c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,
+                use_drop ? P.ltdrop : nullptr, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw);
+  else
+    INCA_LAUNCH(c, k_pass1<false>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,
+                c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
+                nullptr, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw);
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[2], c->stream));
+  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
+  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
+  INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, P.Io);
+  if (use_drop) {
+    INCA_LAUNCH(c, k_sum_drop, nblk(nwt), 256, 0, nwt, P.mwdev, P.nmol, P.dmass, P.Dt);
+    INCA_LAUNCH(c, k_tile_to_points, P.tblk, 256, 0, tiles, nwt, c->d_perm.p, P.Dt, P.Dpt);
+  }
+  // ---- exact thresholds of the outputs
+  if (P.mode == 0) {
+    INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Ms, P.Mo);
+    INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, P.doff, c->d_w.p, P.Io, P.Mo, P.dex);
+    if (use_drop) INCA_LAUNCH(c, k_seg_sums, nseg, 256, 0, nseg, P.doff, c->d_w.p, P.Dpt, P.Dpt, P.ddrop);
+    INCA_LAUNCH(c, k_thr_exact_seg, sblk, 128, 0, nseg, P.dex, P.ddrop, use_drop ? 1 : 0, P.eps, P.tau_scale, P.dT,
+                P.retry);
+  } else if (P.mode == 1) {
+    INCA_CUDA(c, cudaMemsetAsync(P.dmax, 0, 2 * sizeof(unsigned long long), c->stream));
+    INCA_LAUNCH(c, k_absmax2, static_cast<unsigned>(std::min<int64_t>(nblk(ngrid), 4096)), 256, 0, ngrid, P.Is, P.Ms,
+                P.dmax);
+    if (use_drop) {
+      INCA_CUDA(c, cudaMemsetAsync(P.dmax2, 0, 2 * sizeof(unsigned long long), c->stream));
+      INCA_LAUNCH(c, k_absmax2, static_cast<unsigned>(std::min<int64_t>(nblk(nwt), 4096)), 256, 0, nwt, P.Dt, P.Dt,
+                  P.dmax2);
+    }
+    INCA_LAUNCH(c, k_thr_exact_max, 1, 32, 0, P.dmax, P.dmax2, use_drop ? 1 : 0, P.eps, P.tau_scale, P.dT, P.retry);
+  } else {
+    INCA_CUDA(c, cudaMemsetAsync(P.dT, 0, sizeof(double), c->stream));
+  }
+  INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.mode, c->d_perm.p, P.seg_of, P.dT, c->d_w.p, P.Is,
+              P.Ms, P.eps, P.tau_scale, P.fused ? nullptr : P.glt, P.ptau);
+  // sub-tiles where an exact threshold fell below its estimate (the correction pass skips
+  // every item whose tile has none)
+  if (P.fused) INCA_LAUNCH(c, k_band, P.gblk, 256, 0, tiles, P.ngroups, P.ptau, P.ptau_est, P.glt, P.stats + 12);
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[3], c->stream));
+  INCA_LAUNCH(c, k_pass2, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+              c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
+              use_drop ? P.ltdrop : nullptr, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1, P.stats + 4, P.errw);
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[4], c->stream));
+  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.p1, P.p2, P.Is);
+  INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, c->d_ivec.p);
+  if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[5], c->stream));
   INCA_CUDA(c, cudaGetLastError());
-  if (fused) {
-    INCA_LAUNCH(c, k_band, gblk, 256, 0, tiles, ngroups, ptau, ptau_est, glt, stats + 12);
-    unsigned long long nband = 0;
-    INCA_CUDA(c, cudaMemcpyAsync(&nband, stats + 12, sizeof(nband), cudaMemcpyDeviceToHost, c->stream));
-    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-    run_pass2 = nband > 0;
-  }
-  INCA_CUDA(c, cudaEventRecord(ev.e[3], c->stream));
-  if (run_pass2) {
-    INCA_LAUNCH(c, k_pass2, nctas, 32, dsmem, c->d_chunks.p, mwdev, nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p,
-                c->d_plo.p, tiles, wbox, gbox, glt, ptau, fused ? ptau_est : nullptr, use_drop ? ltdrop : nullptr, tab,
-                nitems, stage_floats, p2, work + 1, stats + 4, errw);
-    INCA_CUDA(c, cudaGetLastError());
-  }
-  INCA_CUDA(c, cudaEventRecord(ev.e[4], c->stream));
-  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, mwdev, nmol, p1, run_pass2 ? p2 : nullptr, Is);
-  INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, Is, c->d_ivec.p);
-  INCA_CUDA(c, cudaGetLastError());
-  INCA_CUDA(c, cudaEventRecord(ev.e[5], c->stream));
-  INCA_CUDA(c, cudaEventSynchronize(ev.e[5]));
-  float t12 = 0, t34 = 0, t05 = 0;
-  cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);
-  cudaEventElapsedTime(&t34, ev.e[3], ev.e[4]);
-  cudaEventElapsedTime(&t05, ev.e[0], ev.e[5]);
-  unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int herr = 0;
-  INCA_CUDA(c, cudaMemcpy(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost));
-  INCA_CUDA(c, cudaMemcpy(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost));
+  return INCA_OK;
+}
+
+// After the device work: errors, the retry flag, statistics and (with events) timings.
+int mixed_finish(inca_ctx* c, const MixedPlan& P, Events* ev, bool* retry) {
+  INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+  unsigned long long hs[16] = {};
+  int herr = 0, hretry = 0;
+  INCA_CUDA(c, cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
+  INCA_CUDA(c, cudaMemcpy(&herr, P.errw, sizeof(int), cudaMemcpyDeviceToHost));
+  INCA_CUDA(c, cudaMemcpy(&hretry, P.retry, sizeof(int), cudaMemcpyDeviceToHost));
   if (herr) return set_error(c, INCA_E_TIMEOUT, "inca_eval: a bounded wait for a staged quartet chunk gave up");
-  c->t_total_ms = t05;
-  c->t_kernel_ms = t12;  // the pass over all terms
-  c->t_pass2_ms = t34;   // the correction pass (0 when the one-pass form needed none)
+  *retry = hretry != 0;
+  if (ev) {
+    float t12 = 0, t34 = 0, t05 = 0;
+    cudaEventElapsedTime(&t12, ev->e[1], ev->e[2]);
+    cudaEventElapsedTime(&t34, ev->e[3], ev->e[4]);
+    cudaEventElapsedTime(&t05, ev->e[0], ev->e[5]);
+    c->t_total_ms = t05;
+    c->t_kernel_ms = t12;  // the pass over all terms
+    c->t_pass2_ms = t34;   // the correction pass
+  }
   c->t_kernel_launches = 1;
-  c->t_launches = static_cast<int>(c->launches - launches0);
-  if (fused) {
+  if (P.fused) {
     // one-pass kernel: live pairs, warp rounds of corrections (one corrected term per active
     // lane), exact corrected-term count; correction pass: candidate pairs and corrected terms
     // in warps of 32 points
@@ -1660,6 +1678,85 @@ int eval_mixed(inca_ctx* c, double eps) {
     c->pairs_skip = static_cast<int64_t>(hs[2]);
     c->corrected_points = static_cast<int64_t>(hs[7]) * 32;
   }
+  return INCA_OK;
+}
+
+}  // namespace
+
+int eval_mixed(inca_ctx* c, double eps) {
+  if (c->chunks.empty()) {
+    INCA_CUDA(c, cudaMemsetAsync(c->d_ivec.p, 0, sizeof(double) * c->ngrid, c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return INCA_OK;
+  }
+  const int64_t launches0 = c->launches;
+  MixedPlan P;
+  int st = mixed_plan(c, eps, P);
+  if (st) return st;
+  Events ev;
+  for (auto& e : ev.e) INCA_CUDA(c, cudaEventCreate(&e));
+  bool use_drop = P.fused && P.drop_frac > 0.0, retry = false;
+  if ((st = mixed_launch(c, P, use_drop, &ev))) return st;
+  if ((st = mixed_finish(c, P, &ev, &retry))) return st;
+  if (retry && use_drop) {  // too much was left out: once more without leaving terms out
+    if ((st = mixed_launch(c, P, false, &ev))) return st;
+    if ((st = mixed_finish(c, P, &ev, &retry))) return st;
+  }
+  c->t_launches = static_cast<int>(c->launches - launches0);
+  return INCA_OK;
+}
+
+// The same evaluation replayed from a CUDA graph: the first call for a given grid, set of
+// records, precision and tolerance plans, runs once eagerly and captures the launch sequence;
+// later calls launch the graph (all host decisions made at planning; the one that depends on
+// the data -- repeating without dropping -- is taken after the replay, eagerly).
+int eval_mixed_graph(inca_ctx* c, double eps) {
+  if (c->chunks.empty()) return eval_mixed(c, eps);
+  const void* bufs[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};
+  const bool fresh = c->graph_exec && c->graph_grid == c->grid_version && c->graph_prep == c->prepare_count &&
+                     c->graph_eps == eps && std::equal(bufs, bufs + 4, c->graph_bufs);
+  if (!fresh) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+    int st = eval_mixed(c, eps);  // sizes every buffer and fills every cache first
+    if (st) return st;
+    MixedPlan P;
+    if ((st = mixed_plan(c, eps, P))) return st;
+    cudaGraph_t g = nullptr;
+    INCA_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = c->launches;
+    const int sl = mixed_launch(c, P, P.fused && P.drop_frac > 0.0, nullptr);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->graph_launches = c->launches - l0;
+    if (sl) {
+      if (g) cudaGraphDestroy(g);
+      return sl;
+    }
+    if (e) return cuda_error(c, e, "graph capture");
+    e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e) return cuda_error(c, e, "graph instantiate");
+    c->graph_grid = c->grid_version;
+    c->graph_prep = c->prepare_count;
+    c->graph_eps = eps;
+    c->graph_fused = P.fused;
+    c->graph_drop = P.fused && P.drop_frac > 0.0;
+    const void* now[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};
+    std::copy(now, now + 4, c->graph_bufs);
+    return INCA_OK;  // this call's result came from the eager run
+  }
+  MixedPlan P;
+  int st = mixed_plan(c, eps, P);  // same sizes: carves the same buffers, uploads the same tables
+  if (st) return st;
+  INCA_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+  c->launches += c->graph_launches;
+  bool retry = false;
+  if ((st = mixed_finish(c, P, nullptr, &retry))) return st;
+  if (retry && c->graph_drop) {
+    if ((st = mixed_launch(c, P, false, nullptr))) return st;
+    if ((st = mixed_finish(c, P, nullptr, &retry))) return st;
+  }
+  c->t_launches = static_cast<int>(c->graph_launches);
   return INCA_OK;
 }
 

@@ -566,6 +566,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   c->counts.after_screen1 = static_cast<int64_t>(h_n1);
   c->counts.after_screen2 = nsurv;
   c->prepared = true;
+  ++c->prepare_count;
   c->evaluated = false;
   return INCA_OK;
 }

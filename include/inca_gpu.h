@@ -132,6 +132,13 @@ int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* c
  * stays on the device for the reductions). */
 int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 
+/* inca_eval replayed from a CUDA graph (INCA_MIXED; INCA_FP64 runs as inca_eval). The first
+ * call after the grid, the records (inca_prepare, inca_batch_prepare) or tol change evaluates
+ * normally and captures the evaluation's launch sequence; later calls launch the captured graph,
+ * which runs every pass without returning to the host in between. No counterpart in the
+ * reference. */
+int inca_eval_graph(inca_ctx* ctx, int mode, double tol, double* ivec);
+
 /* Radial integral, Vee and the per-centre TFVC decomposition (mod_intracule.f90:441-455)
  * of the last evaluation on a radial grid. per_centre/vee_per_centre (nquad) may be NULL. */
 int inca_radial_integral(inca_ctx* ctx, double* total, double* vee, double* per_centre,

@@ -88,3 +88,22 @@ def test_cube_one_pass(ctx):
     ref = ctx.eval(mode=0)
     I = ctx.eval(mode=1, tol=1e-8)
     assert np.abs(I - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("grid", ["scan", "cube", "small"])
+def test_graph_replay_matches_eager(ctx, grid):
+    if grid == "scan":
+        ctx.grid_scan(*SCAN)
+    elif grid == "cube":
+        ctx.grid_cube([0.0, 0.0, 0.0], [0.15, 0.15, 0.15], [32, 32, 32])
+    else:
+        ctx.grid_scan([0.0], [2.0], [0.1], [110])  # below the one-pass size: two passes
+    eager = ctx.eval(mode=1, tol=1e-8)
+    first = ctx.eval_graph(mode=1, tol=1e-8)   # captures (this result comes from an eager run)
+    n0 = ctx.kernel_launches()
+    again = ctx.eval_graph(mode=1, tol=1e-8)   # replays
+    third = ctx.eval_graph(mode=1, tol=1e-8)
+    np.testing.assert_array_equal(first, eager)
+    np.testing.assert_array_equal(again, eager)
+    np.testing.assert_array_equal(third, eager)
+    assert ctx.kernel_launches() > n0
