@@ -266,6 +266,146 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
   }
 }
 
+// ---- packed pairs of FP32 values (two points per instruction: add/sub/mul/fma .f32x2, each
+// half rounded exactly as the scalar instruction). Off by default: on the bench workload the
+// packed pass-1 kernel gives bit-identical sums but runs 9 % slower (the per-element steps --
+// rounding, exponent bits, clamps, correction tests -- add register moves).
+#ifndef INCA_F32X2
+#define INCA_F32X2 0
+#endif
+struct P2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ P2 pk(float a, float b) {
+  P2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ P2 pb(float a) { return pk(a, a); }
+__device__ __forceinline__ void up(P2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v)); }
+__device__ __forceinline__ P2 padd(P2 a, P2 b) {
+  P2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ P2 psub(P2 a, P2 b) {
+  P2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ P2 pmul(P2 a, P2 b) {
+  P2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ P2 pfma(P2 a, P2 b, P2 c) {
+  P2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+__device__ __forceinline__ P2 pabs(P2 a) {
+  float x, y;
+  up(a, x, y);
+  return pk(fabsf(x), fabsf(y));
+}
+
+// exp2 of y = -q for two values (q >= 0), bit-identical to exp2_fp32(-q, ks) on each: with
+// g = q + n = -(y - n), the polynomial in f = -g is evaluated in g with the signs of the odd
+// coefficients flipped, which gives the same roundings (negation is exact) and, for degree 7,
+// the same sign at the end.
+__device__ __forceinline__ P2 exp2_neg_x2(P2 q, int ks) {
+  float q0, q1;
+  up(q, q0, q1);
+  const float n0 = rintf(-q0), n1 = rintf(-q1);
+  const P2 g = padd(q, pk(n0, n1));
+  P2 p = pb(-1.5303699910873547e-05f);
+  p = pfma(p, g, pb(0.00015469729260075837f));
+  p = pfma(p, g, pb(-0.0013333478709682822f));
+  p = pfma(p, g, pb(0.00961802527308464f));
+  p = pfma(p, g, pb(-0.05550410971045494f));
+  p = pfma(p, g, pb(0.24022650718688965f));
+  p = pfma(p, g, pb(-0.6931471824645996f));
+  p = pfma(p, g, pb(1.0f));
+  const int e0 = min(max(static_cast<int>(fmaxf(n0, -1000.0f)) + ks + 127, 0), 254);
+  const int e1 = min(max(static_cast<int>(fmaxf(n1, -1000.0f)) + ks + 127, 0), 254);
+  return pmul(p, pk(__int_as_float(e0 << 23), __int_as_float(e1 << 23)));
+}
+
+// Horner of a class-uniform degree for two packed points (loop over the degree).
+template <bool kAbs>
+__device__ __forceinline__ P2 poly_x2(int L, const float* __restrict__ C, P2 u) {
+  P2 v = pb(kAbs ? fabsf(C[0]) : C[0]);
+#pragma unroll 1
+  for (int m = 1; m <= L; ++m) v = pfma(v, u, pb(kAbs ? fabsf(C[m]) : C[m]));
+  return v;
+}
+
+// terms32<4, kErr> with the points in packed pairs (0, 1) and (2, 3): the same operations in the
+// same order, so every term and bound is bit-identical to the scalar form (and to term32_one).
+template <bool kErr>
+__device__ __forceinline__ void terms32_x2(const float* __restrict__ R, const int L[3], const P2 (&rh)[3][2],
+                                           const P2 (&rl)[3][2], P2 (&t)[2], P2 (&err)[2]) {
+  const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
+  const int ks = static_cast<int>(R[11]);
+  P2 u[3][2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const P2 b_hi = pb(R[2 + d]), b_lo = pb(R[5 + d]);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      P2 t1 = pfma(pb(s_lo), rh[d][k], b_lo);
+      t1 = pfma(pb(s_hi), rl[d][k], t1);
+      u[d][k] = padd(pfma(pb(s_hi), rh[d][k], b_hi), t1);
+    }
+  }
+  P2 E[2], Q[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    P2 q = pmul(u[0][k], u[0][k]);
+    q = pfma(u[1][k], u[1][k], q);
+    q = pfma(u[2][k], u[2][k], q);
+    Q[k] = q;
+    E[k] = exp2_neg_x2(q, ks);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        float a, b;
+        up(u[d][k], a, b);
+        u[d][k] = pk(fminf(fmaxf(a, -kUClamp), kUClamp), fminf(fmaxf(b, -kUClamp), kUClamp));
+      }
+    }
+  const float* Cx = R + 12;
+  const float* Cy = Cx + L[0] + 1;
+  const float* Cz = Cy + L[1] + 1;
+  const float* Cd[3] = {Cx, Cy, Cz};
+  P2 P[2] = {E[0], E[1]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) P[k] = pmul(P[k], poly_x2<false>(L[d], Cd[d], u[d][k]));
+    }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) t[k] = pfma(P[k], pb(A_hi), pmul(P[k], pb(A_lo)));
+  if (kErr) {
+    const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
+    const float aA = 5.9604645e-08f * fabsf(A_hi);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) P[k] = pmul(E[k], pfma(Q[k], pb(3.0f * aA), pb(k0 * fabsf(A_hi))));
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (L[d]) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) P[k] = pmul(P[k], poly_x2<true>(L[d], Cd[d], pabs(u[d][k])));
+      }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) err[k] = P[k];
+  }
+}
+
 // The same FP32 term and error bound for one point with loop-based Horner (compact code for
 // the correction pass; same operation sequence and rounding as terms32).
 __device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry,
@@ -615,8 +755,25 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     }
     const TileInfo T = tiles[wtile];
     if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
-    float rh[3][kPPT], rl[3][kPPT];
-    load_points(phi, plo, T, lane, rh, rl);
+    float rhs[3][kPPT], rls[3][kPPT];
+    load_points(phi, plo, T, lane, rhs, rls);
+#if INCA_F32X2
+    P2 rh[3][2], rl[3][2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int k2 = 0; k2 < 2; ++k2) {
+        rh[d][k2] = pk(rhs[d][2 * k2], rhs[d][2 * k2 + 1]);
+        rl[d][k2] = pk(rls[d][2 * k2], rls[d][2 * k2 + 1]);
+      }
+#define INCA_RH(d, p) rhs[d][p]
+#define INCA_RL(d, p) rls[d][p]
+#else
+    float (&rh)[3][kPPT] = rhs;
+    float (&rl)[3][kPPT] = rls;
+#define INCA_RH(d, p) rh[d][p]
+#define INCA_RL(d, p) rl[d][p]
+#endif
     float tau[kPPT];
     f2 corr[kPPT];
     if (kFuse) {
@@ -635,12 +792,17 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     const float thr = (kFuse && lt_drop) ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
     float dm = 0.0f;
     double acc[kPPT];
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) acc[p] = 0.0;
+#if INCA_F32X2
+    P2 sh[2], sl[2], sa[2];
+#pragma unroll
+    for (int k2 = 0; k2 < 2; ++k2) sh[k2] = sl[k2] = sa[k2] = pb(0.0f);
+#else
     float sh[kPPT], sl[kPPT], sa[kPPT];
 #pragma unroll
-    for (int p = 0; p < kPPT; ++p) {
-      acc[p] = 0.0;
-      sh[p] = sl[p] = sa[p] = 0.0f;
-    }
+    for (int p = 0; p < kPPT; ++p) sh[p] = sl[p] = sa[p] = 0.0f;
+#endif
     __syncwarp();
     int nfold = 0;
     bool ok = true;
@@ -664,6 +826,34 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       while (m) {
         const int q = __ffs(m) - 1;
         m &= m - 1;
+#if INCA_F32X2
+        P2 t2[2], e2[2];
+        terms32_x2<true>(st + q * sg.stride32, L, rh, rl, t2, e2);
+#pragma unroll
+        for (int k2 = 0; k2 < 2; ++k2) {
+          if (kFuse) {
+            float ta, tb, ea, eb;
+            up(t2[k2], ta, tb);
+            up(e2[k2], ea, eb);
+            if (ea > tau[2 * k2]) {
+              nm[2 * k2] |= 1u << q;
+              ta = 0.0f;
+            }
+            if (eb > tau[2 * k2 + 1]) {
+              nm[2 * k2 + 1] |= 1u << q;
+              tb = 0.0f;
+            }
+            t2[k2] = pk(ta, tb);
+          }
+          // TwoSum of the pair sums and the term, packed
+          const P2 s2 = padd(sh[k2], t2[k2]);
+          const P2 bb = psub(s2, sh[k2]);
+          const P2 lo = padd(psub(sh[k2], psub(s2, bb)), psub(t2[k2], bb));
+          sh[k2] = s2;
+          sl[k2] = padd(sl[k2], lo);
+          sa[k2] = padd(sa[k2], e2[k2]);
+        }
+#else
         float t[kPPT], e[kPPT];
         terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
 #pragma unroll
@@ -677,6 +867,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           sl[p] = __fadd_rn(sl[p], s2.lo);
           sa[p] = __fadd_rn(sa[p], e[p]);
         }
+#endif
       }
       if (kFuse) {
 #pragma unroll
@@ -689,8 +880,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
             if (!INCA_DF_PAIRS && mm) {
               const int q = __ffs(mm) - 1;
               mm &= mm - 1;
-              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p],
-                                     rl[0][p], rl[1][p], rl[2][p], tab);
+              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], INCA_RH(0, p), INCA_RH(1, p),
+                                     INCA_RH(2, p), INCA_RL(0, p), INCA_RL(1, p), INCA_RL(2, p), tab);
               corr[p] = df_add(corr[p], tdf);
               ++ncorr;
             } else if (mm) {
@@ -699,8 +890,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
               const bool two = mm != 0u;
               const int qb = two ? __ffs(mm) - 1 : qa;
               if (two) mm &= mm - 1;
-              const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], rh[0][p],
-                                      rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
+              const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2],
+                                      INCA_RH(0, p), INCA_RH(1, p), INCA_RH(2, p), INCA_RL(0, p), INCA_RL(1, p),
+                                      INCA_RL(2, p), tab);
               corr[p] = df_add(corr[p], r.a);
               if (two) corr[p] = df_add(corr[p], r.b);
               ncorr += two ? 2 : 1;
@@ -710,6 +902,29 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       }
       // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
       const bool fold = ++nfold == kFold;
+#if INCA_F32X2
+#pragma unroll
+      for (int k2 = 0; k2 < 2; ++k2) {
+        const P2 r = padd(sh[k2], sl[k2]);  // fast TwoSum, packed
+        sl[k2] = psub(sl[k2], psub(r, sh[k2]));
+        sh[k2] = r;
+        if (fold) {
+          float h0, h1, l0, l1;
+          up(sh[k2], h0, h1);
+          up(sl[k2], l0, l1);
+          acc[2 * k2] += static_cast<double>(h0) + static_cast<double>(l0);
+          acc[2 * k2 + 1] += static_cast<double>(h1) + static_cast<double>(l1);
+          sh[k2] = sl[k2] = pb(0.0f);
+        }
+      }
+      if (kFuse && fold) {
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) {
+          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+          corr[p] = {0.0f, 0.0f};
+        }
+      }
+#else
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         const f2 r = fast_two_sum(sh[p], sl[p]);
@@ -724,6 +939,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           }
         }
       }
+#endif
       if (fold) nfold = 0;
       __syncwarp();
     }
@@ -731,14 +947,29 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       if (lane == 0) atomicExch(err, 1);
       break;
     }
+#if INCA_F32X2
+    float shs[kPPT], sls[kPPT], sas[kPPT];
+#pragma unroll
+    for (int k2 = 0; k2 < 2; ++k2) {
+      up(sh[k2], shs[2 * k2], shs[2 * k2 + 1]);
+      up(sl[k2], sls[2 * k2], sls[2 * k2 + 1]);
+      up(sa[k2], sas[2 * k2], sas[2 * k2 + 1]);
+    }
+#else
+    float (&shs)[kPPT] = sh;
+    float (&sls)[kPPT] = sl;
+    float (&sas)[kPPT] = sa;
+#endif
+#undef INCA_RH
+#undef INCA_RL
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
-      acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
+      acc[p] += static_cast<double>(shs[p]) + static_cast<double>(sls[p]);
       if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
       const int j = lane + 32 * p;
       if (j < T.count) {
         part[pat + T.start + j] = acc[p];
-        part_abs[pat + T.start + j] = static_cast<double>(sa[p]);
+        part_abs[pat + T.start + j] = static_cast<double>(sas[p]);
       }
     }
     if (kFuse && drop_mass) {
