@@ -26,6 +26,11 @@ U8P = ctypes.POINTER(ctypes.c_uint8)
 VP = ctypes.c_void_p
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("items_per_cta", ctypes.c_int32), ("sample_stride", ctypes.c_int32),
+                ("estimate_safety", ctypes.c_double), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
+
+
 class Counts(ctypes.Structure):
     _fields_ = [("read", ctypes.c_int64), ("after_screen1", ctypes.c_int64), ("after_screen2", ctypes.c_int64)]
 
@@ -70,6 +75,8 @@ SIGNATURES = {
     "inca_mlp_train": (ctypes.c_int, [VP, ctypes.c_int64, FP, FP, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
                                       ctypes.c_uint64, FP]),
     "inca_eval_graph": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_double, DP]),
+    "inca_autotune": (ctypes.c_int, [VP, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(Tuning)]),
+    "inca_set_tuning": (ctypes.c_int, [VP, ctypes.POINTER(Tuning)]),
     "inca_batch_clear": (ctypes.c_int, [VP]),
     "inca_batch_add_closed_shell": (ctypes.c_int, [VP, ctypes.c_int32, DP, IP, DP, DP, DP, DP, ctypes.c_int,
                                                    ctypes.c_int32, DP, DP, DP, IP, ctypes.c_int, IP]),
@@ -294,6 +301,19 @@ class Context:
         iv = np.zeros(self.ngrid) if copy else None
         self._check(self.lib.inca_eval(self.h, mode, tol, _d(iv)))
         return iv
+
+    def autotune(self, tol=1e-10, reps=3):
+        """Tune the mixed evaluation's schedule on the current grid and records (see inca_autotune)."""
+        t = Tuning()
+        self._check(self.lib.inca_autotune(self.h, tol, reps, ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tuning(self, items_per_cta=None, sample_stride=None, estimate_safety=None):
+        if items_per_cta is None:
+            self._check(self.lib.inca_set_tuning(self.h, None))
+            return
+        t = Tuning(items_per_cta, sample_stride, estimate_safety, 0.0, 0.0)
+        self._check(self.lib.inca_set_tuning(self.h, ctypes.byref(t)))
 
     def eval_graph(self, mode=INCA_MIXED, tol=1e-10, copy=True):
         """inca_eval through a captured CUDA graph (the first call per grid/records/tol captures)."""

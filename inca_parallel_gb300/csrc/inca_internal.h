@@ -206,6 +206,12 @@ struct inca_ctx {
   int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0, corrected_points = 0;
   int64_t launches = 0;  // own kernel launches since creation
 
+  // schedule of the mixed evaluation (inca_autotune / inca_set_tuning; 0 or < 0: defaults)
+  int tune_items_per_cta = 0;
+  int tune_sample_stride = 0;
+  double tune_safety = -1.0;
+  int sample_stride_built = 0;  // stride of the current sorted sample
+
   // graph replay of the mixed evaluation (captured for one grid, set of records and tolerance)
   inca::DevBuf<float2> d_exptab;  // 2^(j/256) table of the double-float exp2
   int64_t prepare_count = 0;      // bumped by every inca_prepare / batch preparation
@@ -231,6 +237,9 @@ int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int b
 
 // intracule_eval.cu
 int eval_device(inca_ctx* c, int mode, double tol, bool graph = false);
+// mixed_eval.cu
+int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc, int* stride, double* safety, double* best_ms,
+                   double* default_ms);
 
 // grid_build.cu
 int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,

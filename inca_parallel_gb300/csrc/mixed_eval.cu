@@ -1517,8 +1517,9 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
 
 // The sorted grid (and, for the one-pass form, the sorted sample), rebuilt when the grid changes.
 int prepare_sorted_grid(inca_ctx* c, bool sample) {
+  const int stride = c->tune_sample_stride > 0 ? c->tune_sample_stride : static_cast<int>(kSampleStride);
   const bool main_ok = c->mix_version == c->grid_version;
-  const bool sample_ok = !sample || c->sample_version == c->grid_version;
+  const bool sample_ok = !sample || (c->sample_version == c->grid_version && c->sample_stride_built == stride);
   if (main_ok && sample_ok) return INCA_OK;
   const int64_t n = c->ngrid;
   // bounding box of the grid (one host copy of the coordinates; cheap next to evaluation)
@@ -1542,10 +1543,11 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
     c->mix_version = c->grid_version;
   }
   if (!sample_ok) {
-    const int st = sort_points(c, kSampleStride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
+    const int st = sort_points(c, stride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
                                c->d_tiles_s, &c->nsample, &c->ntiles_s, c->mol_span_s);
     if (st) return st;
     c->sample_version = c->grid_version;
+    c->sample_stride_built = stride;
   }
   return INCA_OK;
 }
@@ -1586,9 +1588,9 @@ std::vector<float2> exp2_table() {
 // proportion to its tiles x chunks, about kItemsPerCta work items per resident CTA in total
 // (an item is then small next to the whole pass, so the CTAs finish together).
 std::vector<MolWork> work_table(const std::vector<MolSpan>& sp, const std::vector<ChunkRange>& ch, int num_sms,
-                                int64_t* nitems, int64_t* npart, int64_t* ndrop) {
+                                int items_per_cta, int64_t* nitems, int64_t* npart, int64_t* ndrop) {
   const int nmol = static_cast<int>(sp.size());
-  const double target = double(num_sms) * INCA_PASS_CTAS_PER_SM * kItemsPerCta;
+  const double target = double(num_sms) * INCA_PASS_CTAS_PER_SM * items_per_cta;
   double total = 0.0;
   for (int m = 0; m < nmol; ++m) total += double(sp[m].ntiles) * std::max(ch[m].end - ch[m].begin, 0);
   std::vector<MolWork> w(nmol);
@@ -1665,17 +1667,19 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   // knobs (environment, read per evaluation; tuning and test aids)
   P.tau_scale = env_knob("INCA_TAU_SCALE", kTauScale, 1e-300, HUGE_VAL);
   P.drop_frac = env_knob("INCA_DROP_FRACTION", kDropFrac, 0.0, 0.5);
-  P.safety = env_knob("INCA_EST_SAFETY", kEstSafety, 0.0, HUGE_VAL);
+  P.safety = env_knob("INCA_EST_SAFETY", c->tune_safety >= 0.0 ? c->tune_safety : kEstSafety, 0.0, HUGE_VAL);
   P.nwt = c->ntiles;
   P.ngroups = P.nwt * kPPT;
-  const std::vector<MolWork> hmw = work_table(c->mol_span, c->mol_chunks, c->num_sms, &P.nitems, &P.npart, &P.ndrop);
+  const int ipc = c->tune_items_per_cta > 0 ? c->tune_items_per_cta : kItemsPerCta;
+  const std::vector<MolWork> hmw =
+      work_table(c->mol_span, c->mol_chunks, c->num_sms, ipc, &P.nitems, &P.npart, &P.ndrop);
   P.nmol = static_cast<int>(hmw.size());
   P.nctas = persistent_ctas(P.nitems, c->num_sms);
   std::vector<MolWork> hmw_s;
   if (P.fused) {
     P.ns = c->nsample;
     int64_t ndrop_s = 0;
-    hmw_s = work_table(c->mol_span_s, c->mol_chunks, c->num_sms, &P.nitems_s, &P.npart_s, &ndrop_s);
+    hmw_s = work_table(c->mol_span_s, c->mol_chunks, c->num_sms, ipc, &P.nitems_s, &P.npart_s, &ndrop_s);
     P.nctas_s = persistent_ctas(P.nitems_s, c->num_sms);
   }
   // survivors of the largest molecule: an upper bound on the terms left out at a point
@@ -1941,6 +1945,74 @@ int eval_mixed(inca_ctx* c, double eps) {
 // records, precision and tolerance plans, runs once eagerly and captures the launch sequence;
 // later calls launch the graph (all host decisions made at planning; the one that depends on
 // the data -- repeating without dropping -- is taken after the replay, eagerly).
+// Schedule tuning by coordinate descent over (items per CTA, sample stride, estimate safety):
+// every candidate is a complete mixed evaluation on the current grid and records, timed with
+// CUDA events (median of `reps` after one untimed run); a candidate replaces the best only when
+// it is at least 1% faster, so timing noise does not move the choice. The fastest stays in the
+// context. All candidates meet the tolerance, so the choice changes only the time. On an error
+// the context's previous schedule is restored.
+int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_out, double* safety_out,
+                   double* best_ms, double* default_ms) {
+  const int saved_ipc = c->tune_items_per_cta, saved_stride = c->tune_sample_stride;
+  const double saved_safety = c->tune_safety;
+  auto timed = [&](int ipc, int stride, double safety, double* ms) -> int {
+    c->tune_items_per_cta = ipc;
+    c->tune_sample_stride = stride;
+    c->tune_safety = safety;
+    std::vector<double> t;
+    for (int r = 0; r < reps + 1; ++r) {
+      const int st = eval_mixed(c, eps);
+      if (st) {
+        c->tune_items_per_cta = saved_ipc;
+        c->tune_sample_stride = saved_stride;
+        c->tune_safety = saved_safety;
+        return st;
+      }
+      if (r) t.push_back(c->t_total_ms);
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return INCA_OK;
+  };
+  int ipc = kItemsPerCta, stride = static_cast<int>(kSampleStride);
+  double safety = kEstSafety, best = 0.0;
+  int st = timed(ipc, stride, safety, &best);
+  if (st) return st;
+  *default_ms = best;
+  const int ipcs[] = {4, 8, 12, 24, 48};
+  const int strides[] = {8, 16, 32};
+  const double safeties[] = {0.3, 0.5, 0.7};
+  auto better = [&](double ms) { return ms < 0.99 * best; };
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int v : ipcs) {
+      if (v == ipc) continue;
+      double ms;
+      if ((st = timed(v, stride, safety, &ms))) return st;
+      if (better(ms)) { best = ms; ipc = v; }
+    }
+    for (int v : strides) {
+      if (v == stride) continue;
+      double ms;
+      if ((st = timed(ipc, v, safety, &ms))) return st;
+      if (better(ms)) { best = ms; stride = v; }
+    }
+    for (double v : safeties) {
+      if (v == safety) continue;
+      double ms;
+      if ((st = timed(ipc, stride, v, &ms))) return st;
+      if (better(ms)) { best = ms; safety = v; }
+    }
+  }
+  c->tune_items_per_cta = ipc;
+  c->tune_sample_stride = stride;
+  c->tune_safety = safety;
+  *ipc_out = ipc;
+  *stride_out = stride;
+  *safety_out = safety;
+  *best_ms = best;
+  return INCA_OK;
+}
+
 int eval_mixed_graph(inca_ctx* c, double eps) {
   if (c->chunks.empty()) return eval_mixed(c, eps);
   const void* bufs[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};

@@ -132,6 +132,23 @@ int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* c
  * stays on the device for the reductions). */
 int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 
+/* Schedule of the mixed evaluation: work items per resident CTA of the persistent passes,
+ * the stride of the grid sample that estimates the thresholds, and the factor applied to the
+ * estimates. inca_autotune times complete INCA_MIXED evaluations of the current grid and records
+ * (median of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
+ * context and reports it with the time of the default schedule; the last evaluation's results
+ * stay on the device. inca_set_tuning sets a schedule (NULL: the defaults). Every schedule meets
+ * the tolerance. No counterpart in the reference. */
+typedef struct inca_tuning {
+  int32_t items_per_cta;
+  int32_t sample_stride;
+  double estimate_safety;
+  double best_ms;     /* output of inca_autotune */
+  double default_ms;  /* output of inca_autotune */
+} inca_tuning;
+int inca_autotune(inca_ctx* ctx, double tol, int32_t reps, inca_tuning* chosen);
+int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);
+
 /* inca_eval replayed from a CUDA graph (INCA_MIXED; INCA_FP64 runs as inca_eval). The first
  * call after the grid, the records (inca_prepare, inca_batch_prepare) or tol change evaluates
  * normally and captures the evaluation's launch sequence; later calls launch the captured graph,

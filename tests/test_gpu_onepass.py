@@ -107,3 +107,24 @@ def test_graph_replay_matches_eager(ctx, grid):
     np.testing.assert_array_equal(again, eager)
     np.testing.assert_array_equal(third, eager)
     assert ctx.kernel_launches() > n0
+
+
+def test_autotune_keeps_tolerance(ctx, scan_fp64):
+    ctx.grid_scan(*SCAN)
+    t = ctx.autotune(tol=1e-8, reps=2)
+    assert t["items_per_cta"] in (4, 8, 12, 24, 48)
+    assert t["sample_stride"] in (8, 16, 32)
+    assert t["estimate_safety"] in (0.3, 0.5, 0.7)
+    assert 0 < t["best_ms"] <= t["default_ms"]
+    try:
+        # the tuned schedule stays in the context; every schedule meets the tolerance
+        I = _scan_mixed(ctx)
+        rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+        assert rel.max() <= 1e-8, rel.max()
+        for ipc, stride, safety in ((4, 32, 0.3), (48, 8, 0.7)):
+            ctx.set_tuning(ipc, stride, safety)
+            I = _scan_mixed(ctx)
+            rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+            assert rel.max() <= 1e-8, (ipc, stride, safety, rel.max())
+    finally:
+        ctx.set_tuning()
