@@ -49,7 +49,10 @@ int choose_splits(int64_t tiles, int64_t nchunks, int num_sms, int ctas_per_sm);
 
 namespace {
 
-constexpr int kPPT = 4;                 // points per lane
+#ifndef INCA_PPT
+#define INCA_PPT 4
+#endif
+constexpr int kPPT = INCA_PPT;          // points per lane
 constexpr int kWarpTile = 32 * kPPT;    // 128 points per CTA (one warp)
 constexpr int kMaxStride32 = (12 + 2 * 3 * kMaxCoef + 3) & ~3;
 constexpr int kChunkMax = 32;
@@ -86,27 +89,53 @@ constexpr int kItemsPerCta = 12;         // persistent passes: work items per re
 #ifndef INCA_DF_PAIRS
 #define INCA_DF_PAIRS 1
 #endif
+// coefficient prefetch in the Horner loops of the pass-1 term evaluation
+#ifndef INCA_POLY_PF
+#define INCA_POLY_PF 0
+#endif
+// 16-byte loads of the record head in the pass-1 term evaluation
+#ifndef INCA_REC_VEC
+#define INCA_REC_VEC 1
+#endif
 
 // 2^y for y <= 0 in FP32 without systematic bias: y = n + f (n = rint(y), |f| <= 1/2),
-// 2^f by a degree-7 polynomial (Chebyshev interpolation of 2^x on [-1/2, 1/2], relative
-// approximation error 3.2e-9) evaluated by FMA Horner (<= 1.1 ulp), times 2^n built from the
-// exponent bits (exact; 0 below 2^-126). The hardware ex2.approx was measured biased by
-// -5e-8 relative on this range, which the error model of the correction pass cannot absorb.
-// ks: an integer power of two applied exactly in the final scaling (2^(y + ks)).
+// 2^f by a polynomial evaluated by FMA Horner, times 2^(n + ks) built from the exponent bits
+// (exact; 0 below 2^-126). ks: an integer power of two applied exactly in the final scaling.
+// Polynomials (coefficients highest degree first, FP32): degree 6, minimax relative
+// approximation of 2^x on [-1/2, 1/2] (1.9e-9; with the FP32 Horner steps 7.9e-8 = 1.32 u32
+// measured over 2e6 points, mean 2.6e-10); degree 7 (INCA_EXP2_DEG=7), Chebyshev interpolation
+// (3.2e-9; 6.8e-8 = 1.13 u32 with Horner). The error bound of a term allows 2 u32 for E. The
+// hardware ex2.approx was measured biased by -5e-8 relative on this range, which the error
+// model of the correction pass cannot absorb.
+// Rounding: y is clamped to [-1000, 0] (below -1000 the scale is zero for every ks used here)
+// and t = y + 1.5 * 2^23 rounds it to an integer in the low mantissa bits (ties to even, as
+// rint), so n = t - 1.5 * 2^23 and f = y - n are exact and the exponent field is the integer
+// bits of t plus a per-record constant: no conversion instructions.
+#ifndef INCA_EXP2_DEG
+#define INCA_EXP2_DEG 6
+#endif
+#if INCA_EXP2_DEG == 6
+constexpr int kExp2Deg = 6;
+__device__ constexpr float kExp2C[7] = {1.534581242594868e-4f, 1.3399930903688073e-3f, 9.618489071726799e-3f,
+                                        5.550328642129898e-2f, 0.24022646248340607f, 0.6931471824645996f, 1.0f};
+#else
+constexpr int kExp2Deg = 7;
+__device__ constexpr float kExp2C[8] = {1.5303699910873547e-05f, 0.00015469729260075837f, 0.0013333478709682822f,
+                                        0.00961802527308464f,    0.05550410971045494f,    0.24022650718688965f,
+                                        0.6931471824645996f,     1.0f};
+#endif
+constexpr float kRoundShift = 12582912.0f;  // 1.5 * 2^23
+constexpr int kRoundShiftBits = 0x4B400000;
+
 __device__ __forceinline__ float exp2_fp32(float y, int ks) {
-  const float n = rintf(y);
-  const float f = __fsub_rn(y, n);
-  float p = 1.5303699910873547e-05f;
-  p = __fmaf_rn(p, f, 0.00015469729260075837f);
-  p = __fmaf_rn(p, f, 0.0013333478709682822f);
-  p = __fmaf_rn(p, f, 0.00961802527308464f);
-  p = __fmaf_rn(p, f, 0.05550410971045494f);
-  p = __fmaf_rn(p, f, 0.24022650718688965f);
-  p = __fmaf_rn(p, f, 0.6931471824645996f);
-  p = __fmaf_rn(p, f, 1.0f);
-  // n is clamped in FP32 before the integer conversion (an out-of-range conversion has no
-  // defined result); below -1000 the scale is zero for any ks used here
-  const int e = min(max(static_cast<int>(fmaxf(n, -1000.0f)) + ks + 127, 0), 254);
+  const float yc = fmaxf(y, -1000.0f);
+  const float t = __fadd_rn(yc, kRoundShift);
+  const float n = __fsub_rn(t, kRoundShift);
+  const float f = __fsub_rn(yc, n);
+  float p = kExp2C[0];
+#pragma unroll
+  for (int i = 1; i <= kExp2Deg; ++i) p = __fmaf_rn(p, f, kExp2C[i]);
+  const int e = min(max(__float_as_int(t) + (ks + 127 - kRoundShiftBits), 0), 254);
   return __fmul_rn(p, __int_as_float(e << 23));
 }
 
@@ -169,12 +198,26 @@ __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, con
   const float c0 = kAbs ? fabsf(C[0]) : C[0];
 #pragma unroll
   for (int p = 0; p < NP; ++p) v[p] = c0;
+#if INCA_POLY_PF
+  // the next coefficient is loaded one step ahead (C[L + 1] is still inside the record: the
+  // coefficient lists are followed by their low parts)
+  float c = C[1];
+#pragma unroll 1
+  for (int m = 1; m <= L; ++m) {
+    const float cn = C[m + 1];
+    const float ca = kAbs ? fabsf(c) : c;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], kAbs ? fabsf(u[p]) : u[p], ca);
+    c = cn;
+  }
+#else
 #pragma unroll 1
   for (int m = 1; m <= L; ++m) {
     const float c = kAbs ? fabsf(C[m]) : C[m];
 #pragma unroll
     for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], kAbs ? fabsf(u[p]) : u[p], c);
   }
+#endif
 }
 
 // The FP32 term of quartet record R at NP points, and a bound e on its rounding error:
@@ -186,12 +229,23 @@ __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, con
 template <int NP, bool kErr>
 __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
                                         const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
+#if INCA_REC_VEC
+  // the record head in three 16-byte loads (records are 16-byte aligned: strides of 4 floats)
+  const float4 R0 = *reinterpret_cast<const float4*>(R);
+  const float4 R1 = *reinterpret_cast<const float4*>(R + 4);
+  const float4 R2 = *reinterpret_cast<const float4*>(R + 8);
+  const float s_hi = R0.x, s_lo = R0.y, A_hi = R2.x, A_lo = R2.y;
+  const int ks = static_cast<int>(R2.w);
+  const float bh[3] = {R0.z, R0.w, R1.x}, bl[3] = {R1.y, R1.z, R1.w};
+#else
   const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
   const int ks = static_cast<int>(R[11]);
+  const float bh[3] = {R[2], R[3], R[4]}, bl[3] = {R[5], R[6], R[7]};
+#endif
   float u[3][NP];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const float b_hi = R[2 + d], b_lo = R[5 + d];
+    const float b_hi = bh[d], b_lo = bl[d];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       float t1 = __fmaf_rn(s_lo, rh[d][p], b_lo);
@@ -310,24 +364,21 @@ __device__ __forceinline__ P2 pabs(P2 a) {
 }
 
 // exp2 of y = -q for two values (q >= 0), bit-identical to exp2_fp32(-q, ks) on each: with
-// g = q + n = -(y - n), the polynomial in f = -g is evaluated in g with the signs of the odd
-// coefficients flipped, which gives the same roundings (negation is exact) and, for degree 7,
-// the same sign at the end.
+// g = q + n = -(y - n) = -f, the Horner steps in f are evaluated in g with the coefficient of
+// degree k multiplied by (-1)^k, which gives the same roundings (negation is exact and
+// rounding is odd-symmetric) and the same sign at the end (degree 0).
 __device__ __forceinline__ P2 exp2_neg_x2(P2 q, int ks) {
   float q0, q1;
   up(q, q0, q1);
-  const float n0 = rintf(-q0), n1 = rintf(-q1);
-  const P2 g = padd(q, pk(n0, n1));
-  P2 p = pb(-1.5303699910873547e-05f);
-  p = pfma(p, g, pb(0.00015469729260075837f));
-  p = pfma(p, g, pb(-0.0013333478709682822f));
-  p = pfma(p, g, pb(0.00961802527308464f));
-  p = pfma(p, g, pb(-0.05550410971045494f));
-  p = pfma(p, g, pb(0.24022650718688965f));
-  p = pfma(p, g, pb(-0.6931471824645996f));
-  p = pfma(p, g, pb(1.0f));
-  const int e0 = min(max(static_cast<int>(fmaxf(n0, -1000.0f)) + ks + 127, 0), 254);
-  const int e1 = min(max(static_cast<int>(fmaxf(n1, -1000.0f)) + ks + 127, 0), 254);
+  q0 = fminf(q0, 1000.0f);
+  q1 = fminf(q1, 1000.0f);
+  const float t0 = __fadd_rn(-q0, kRoundShift), t1 = __fadd_rn(-q1, kRoundShift);
+  const P2 g = padd(pk(q0, q1), pk(__fsub_rn(t0, kRoundShift), __fsub_rn(t1, kRoundShift)));
+  P2 p = pb((kExp2Deg & 1) ? -kExp2C[0] : kExp2C[0]);
+#pragma unroll
+  for (int i = 1; i <= kExp2Deg; ++i) p = pfma(p, g, pb(((kExp2Deg - i) & 1) ? -kExp2C[i] : kExp2C[i]));
+  const int e0 = min(max(__float_as_int(t0) + (ks + 127 - kRoundShiftBits), 0), 254);
+  const int e1 = min(max(__float_as_int(t1) + (ks + 127 - kRoundShiftBits), 0), 254);
   return pmul(p, pk(__int_as_float(e0 << 23), __int_as_float(e1 << 23)));
 }
 
@@ -991,7 +1042,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
 }
 
 // ---------------------------------------------------------------- pass 2 (corrections)
-__global__ void __launch_bounds__(32, 16)
+__global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
