@@ -66,7 +66,10 @@ constexpr double kTestScale = 1.0 / 1.01;  // correct when e > tau / 1.01
 // the largest sampled error sum times kCubeMargin standing in for each point's); where the
 // exact thresholds after the pass are lower than the estimates, a correction pass covers the
 // difference.
-constexpr int64_t kFuseMinPoints = 16384;
+// (2 048: on the 3 050-point CH4 radial-integral grid at 1e-10 the one-pass form takes 3.1 ms
+// in its evaluation pass against 1.1 + 4.2 ms for the two passes; every 16th point still gives
+// a usable estimate, and the exact thresholds and the band pass keep the tolerance regardless)
+constexpr int64_t kFuseMinPoints = 2048;
 constexpr int64_t kSampleStride = 16;
 constexpr double kEstSafety = 0.5;
 constexpr double kCubeMargin = 2.0;
@@ -1421,29 +1424,59 @@ __global__ void k_tile_to_points(const TileInfo* __restrict__ tiles, int64_t nwt
 
 // Sum over the splits of each sorted point (partials laid out per molecule), in split order;
 // b (optional) has the same layout and is added after a.
-__global__ void k_sum_mol(int64_t n, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ a,
-                          const double* __restrict__ b, double* out) {
-  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (i >= n) return;
-  const MolWork W = mw[mol_of_point(mw, nmol, i)];
-  const int64_t at = W.poff + (i - W.p0);
+// Sums over the split partials of each point (k_sum_mol) or tile (k_sum_drop) in a fixed
+// order, so results are reproducible bit for bit: kSumLanes threads per output each add every
+// kSumLanes-th split in increasing order, then the kSumLanes partial sums are added in thread
+// order. (A small grid has few points and up to 4096 splits; one thread per output adding them
+// one after the other waited on memory latency for milliseconds.) Block: 32 outputs x kSumLanes.
+constexpr int kSumLanes = 16;
+__global__ void __launch_bounds__(32 * kSumLanes)
+k_sum_mol(int64_t n, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ a,
+          const double* __restrict__ b, double* out) {
+  __shared__ double sh[kSumLanes][33];
+  const int64_t i = blockIdx.x * 32LL + threadIdx.x;
+  const int y = threadIdx.y;
   double s = 0.0;
-  for (int k = 0; k < W.nsplit; ++k) s += a[at + static_cast<int64_t>(k) * W.np];
-  if (b)
-    for (int k = 0; k < W.nsplit; ++k) s += b[at + static_cast<int64_t>(k) * W.np];
-  out[i] = s;
+  if (i < n) {
+    const MolWork W = mw[mol_of_point(mw, nmol, i)];
+    const int64_t at = W.poff + (i - W.p0);
+    for (int k = y; k < W.nsplit; k += kSumLanes) s += a[at + static_cast<int64_t>(k) * W.np];
+    if (b)
+      for (int k = y; k < W.nsplit; k += kSumLanes) s += b[at + static_cast<int64_t>(k) * W.np];
+  }
+  sh[y][threadIdx.x] = s;
+  __syncthreads();
+  if (y == 0 && i < n) {
+    double t = sh[0][threadIdx.x];
+#pragma unroll
+    for (int r = 1; r < kSumLanes; ++r) t += sh[r][threadIdx.x];
+    out[i] = t;
+  }
 }
 
 // Left-out bound mass of each tile: sum over its molecule's splits.
-__global__ void k_sum_drop(int64_t ntiles, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ d,
-                           double* out) {
-  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (t >= ntiles) return;
-  const MolWork W = mw[mol_of_tile(mw, nmol, t)];
+__global__ void __launch_bounds__(32 * kSumLanes)
+k_sum_drop(int64_t ntiles, const MolWork* __restrict__ mw, int nmol, const double* __restrict__ d, double* out) {
+  __shared__ double sh[kSumLanes][33];
+  const int64_t t = blockIdx.x * 32LL + threadIdx.x;
+  const int y = threadIdx.y;
   double s = 0.0;
-  for (int k = 0; k < W.nsplit; ++k) s += d[W.doff + static_cast<int64_t>(k) * W.ntiles + (t - W.tile0)];
-  out[t] = s;
+  if (t < ntiles) {
+    const MolWork W = mw[mol_of_tile(mw, nmol, t)];
+    for (int k = y; k < W.nsplit; k += kSumLanes)
+      s += d[W.doff + static_cast<int64_t>(k) * W.ntiles + (t - W.tile0)];
+  }
+  sh[y][threadIdx.x] = s;
+  __syncthreads();
+  if (y == 0 && t < ntiles) {
+    double r0 = sh[0][threadIdx.x];
+#pragma unroll
+    for (int r = 1; r < kSumLanes; ++r) r0 += sh[r][threadIdx.x];
+    out[t] = r0;
+  }
 }
+inline unsigned nblk32(int64_t n) { return static_cast<unsigned>((n + 31) / 32); }
+const dim3 kSumBlock(32, kSumLanes);
 
 // ---- thresholds of the outputs, on the device (no host round trip between the passes)
 // The threshold of an output: 3 sigma of the uncorrected rounding errors within the absolute
@@ -1710,8 +1743,9 @@ struct MixedPlan {
 int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   P.ngrid = c->ngrid;
   const int64_t ngrid = P.ngrid;
+  const double fuse_min = env_knob("INCA_FUSE_MIN_POINTS", static_cast<double>(kFuseMinPoints), 256.0, HUGE_VAL);
   P.fused = (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN || c->grid_kind == GRID_CUBE) &&
-            ngrid >= kFuseMinPoints;
+            static_cast<double>(ngrid) >= fuse_min;
   int st = prepare_sorted_grid(c, P.fused);
   if (st) return st;
   P.eps = eps;
@@ -1848,8 +1882,8 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
     INCA_LAUNCH(c, k_pass1<false>, P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, P.nitems_s, P.stage_floats, nullptr,
                 nullptr, nullptr, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw);
-    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
-    INCA_LAUNCH(c, k_sum_mol, nblk(ns), 256, 0, ns, P.mws, P.nmol, P.qabs, nullptr, P.Mss);
+    INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
+    INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.qabs, nullptr, P.Mss);
     if (P.mode == 0) {
       INCA_CUDA(c, cudaMemsetAsync(P.Ios, 0, sizeof(double) * ngrid, c->stream));
       INCA_CUDA(c, cudaMemsetAsync(P.Mos, 0, sizeof(double) * ngrid, c->stream));
@@ -1886,11 +1920,11 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
                 c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
                 nullptr, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[2], c->stream));
-  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
-  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
+  INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
+  INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, P.Io);
   if (use_drop) {
-    INCA_LAUNCH(c, k_sum_drop, nblk(nwt), 256, 0, nwt, P.mwdev, P.nmol, P.dmass, P.Dt);
+    INCA_LAUNCH(c, k_sum_drop, nblk32(nwt), kSumBlock, 0, nwt, P.mwdev, P.nmol, P.dmass, P.Dt);
     INCA_LAUNCH(c, k_tile_to_points, P.tblk, 256, 0, tiles, nwt, c->d_perm.p, P.Dt, P.Dpt);
   }
   // ---- exact thresholds of the outputs
@@ -1923,7 +1957,7 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
               c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
               use_drop ? P.ltdrop : nullptr, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1, P.stats + 4, P.errw);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[4], c->stream));
-  INCA_LAUNCH(c, k_sum_mol, nblk(ngrid), 256, 0, ngrid, P.mwdev, P.nmol, P.p1, P.p2, P.Is);
+  INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, P.p2, P.Is);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, c->d_ivec.p);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[5], c->stream));
   INCA_CUDA(c, cudaGetLastError());

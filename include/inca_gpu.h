@@ -183,7 +183,7 @@ int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
 
 /* Work split of the last INCA_MIXED evaluation, in (quartet, 128-point tile) pairs: evaluated
  * in FP32, examined for corrections (the precise tier; in the one-pass form used on grids of
- * 16 384 points or more, the warp rounds of inline corrections plus the pairs examined by a
+ * 2 048 points or more, the warp rounds of inline corrections plus the pairs examined by a
  * correction pass, if one ran), skipped (bound below 2^-120); and the number of (quartet,
  * point) terms re-evaluated in double-float arithmetic (a correction pass counts them in warps
  * of 32 points). The FP64 form reports zeros. Pointers may be NULL. */

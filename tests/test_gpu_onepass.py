@@ -1,4 +1,4 @@
-"""One-pass mixed evaluation (grids of at least 16 384 points) against the FP64 GPU form.
+"""One-pass mixed evaluation (grids of at least 2 048 points) against the FP64 GPU form.
 
 The FP64 GPU form is checked against the oracle at 1e-12 in test_gpu_parity.py and serves as
 the full-size oracle here. Tolerances: 1e-8 relative on each I(s), 1e-10 relative on the radial
