@@ -34,6 +34,8 @@ THRESH = 1e-12
 SCAN = dict(start=[0.0], end=[10.0], step=[0.05], nang=[590])
 TOL_SCAN = 1e-8
 TOL_INTEGRAL = 1e-10
+TOL_CUBE = 1e-8
+CUBE = ([0.0, 0.0, 0.0], [0.15, 0.15, 0.15], [48, 48, 48])
 
 
 def parse():
@@ -251,6 +253,26 @@ def gpu_arm(args):
         ri[name] = {"ms": statistics.mean(ts), "value": val}
     ri_rel = abs(ri["mixed"]["value"] - ri["fp64"]["value"]) / abs(ri["fp64"]["value"])
 
+    # vector cube (cubeintra lattice, 48^3 at 0.15 bohr): the FP64 form against INCA_MIXED, which
+    # takes the separable double-float form on a lattice
+    ctx.grid_cube(*CUBE)
+    cube = {}
+    for name, mode in (("fp64", INCA_FP64), ("mixed", INCA_MIXED)):
+        ts = []
+        for i in range(3 if mode == INCA_MIXED else 2):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.eval(mode=mode, tol=TOL_CUBE, copy=False)
+            e1.record(stream)
+            e1.synchronize()
+            if i:
+                ts.append(e0.elapsed_time(e1))
+        cube[name] = {"ms": statistics.mean(ts), "I": ctx.eval(mode=mode, tol=TOL_CUBE)}
+    cube_err = float(np.abs(cube["mixed"]["I"] - cube["fp64"]["I"]).max() / np.abs(cube["fp64"]["I"]).max())
+    cube_qp = counts[2] * int(np.prod(CUBE[2]))
+
     # end to end through the C ABI with host buffers (the driver's call sequence)
     ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
     h2d = int(ijkl.nbytes + v.nbytes + b["alpha"].nbytes * 4 + b["tmn"].nbytes)
@@ -315,7 +337,11 @@ def gpu_arm(args):
                        "tiers": stats,
                        "radial_integral_nrad50_nang110": {"fp64_ms": ri["fp64"]["ms"], "mixed_ms": ri["mixed"]["ms"],
                                                           "rel_err": ri_rel, "value": ri["fp64"]["value"],
-                                                          "tolerance": TOL_INTEGRAL}},
+                                                          "tolerance": TOL_INTEGRAL},
+                       "vector_cube_48": {"fp64_ms": cube["fp64"]["ms"], "mixed_ms": cube["mixed"]["ms"],
+                                          "mixed_value": cube_qp / (cube["mixed"]["ms"] * 1e-3),
+                                          "max_err_rel_max": cube_err, "tolerance": TOL_CUBE,
+                                          "form": "separable double-float lattice factors (k_cube_sep)"}},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "T FP32-ops/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_pass1 (one-pass evaluation)", "kernel_ms_per_launch": kms,

@@ -27,6 +27,7 @@ UNITS = {
     "quartet_prep.cu": ["-fmad=false"],
     "intracule_eval.cu": [],
     "mixed_eval.cu": [],
+    "cube_eval.cu": [],
     "grid_build.cu": ["-fmad=false"],
     "noalloc_eval.cu": [],
     "peak_probe.cu": [],
@@ -52,7 +53,7 @@ def _newer(target, deps):
 
 
 def _headers():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")] + \
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))] + \
            [os.path.join(INCLUDE, "inca_gpu.h")]
 
 

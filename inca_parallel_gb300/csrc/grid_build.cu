@@ -484,6 +484,7 @@ int grid_cube_device(inca_ctx* c, const double* center, const double* step, cons
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->grid_kind = GRID_CUBE;
+  for (int i = 0; i < 3; ++i) c->cube_np[i] = np[i];
   c->ngrid = n;
   c->rgrid = n;
   c->maxgrid = n;

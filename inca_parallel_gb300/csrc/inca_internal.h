@@ -168,6 +168,7 @@ struct inca_ctx {
   int64_t ngrid = 0, maxgrid = 0, rgrid = 0;
   int nquad = 0;
   int nradi = 0;
+  int cube_np[3] = {0, 0, 0};    // lattice points per axis (cube grids)
   std::vector<int> h_smn;        // points per shell (scan grids)
   std::vector<double> h_radi;    // shell radii (scan grids)
   std::vector<double> h_cent;    // centres (radial grids)
@@ -195,6 +196,11 @@ struct inca_ctx {
   int64_t ntiles_s = 0;
   std::vector<inca::MolSpan> mol_span_s;
   inca::DevBuf<unsigned char> d_scratch_s;
+
+  // separable cube evaluation: the lattice's axis coordinates (x, y, z runs; rebuilt when the
+  // grid changes)
+  inca::DevBuf<double> d_cube_axes;
+  int64_t cube_axes_version = -1;
 
   // scratch
   inca::DevBuf<double> d_partial;
@@ -240,6 +246,10 @@ int eval_device(inca_ctx* c, int mode, double tol, bool graph = false);
 // mixed_eval.cu
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc, int* stride, double* safety, double* best_ms,
                    double* default_ms);
+int ensure_exp_table(inca_ctx* c);
+// cube_eval.cu
+bool cube_separable(const inca_ctx* c);
+int eval_cube_separable(inca_ctx* c);
 
 // grid_build.cu
 int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,

@@ -129,7 +129,10 @@ int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* c
 /* Evaluate I at every point of the resident grid (mod_intracule.f90:345-358, all quartets).
  * mode: INCA_FP64 or INCA_MIXED; tol: relative tolerance of the mixed form on the grid's
  * outputs (ignored for INCA_FP64; <= 0 selects 1e-10). ivec (ngrid) may be NULL (result
- * stays on the device for the reductions). */
+ * stays on the device for the reductions). On a cube lattice (inca_grid_cube, one molecule)
+ * INCA_MIXED evaluates the lattice's separable factors in double-float (about 2^-44 relative
+ * per term, whatever tol asks for); the environment variable INCA_CUBE_SEPARABLE=0 selects the
+ * general mixed form there instead. */
 int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 
 /* Schedule of the mixed evaluation: work items per resident CTA of the persistent passes,
@@ -152,7 +155,8 @@ int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);
 /* inca_eval replayed from a CUDA graph (INCA_MIXED; INCA_FP64 runs as inca_eval). The first
  * call after the grid, the records (inca_prepare, inca_batch_prepare) or tol change evaluates
  * normally and captures the evaluation's launch sequence; later calls launch the captured graph,
- * which runs every pass without returning to the host in between. No counterpart in the
+ * which runs every pass without returning to the host in between. Cube lattices evaluated by
+ * the separable form (two launches, nothing to plan) run as inca_eval. No counterpart in the
  * reference. */
 int inca_eval_graph(inca_ctx* ctx, int mode, double tol, double* ivec);
 

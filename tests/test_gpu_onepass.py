@@ -83,7 +83,9 @@ def test_radial_integral_one_pass(ctx, ch4):
     assert abs(tot - 45.0) < 0.1
 
 
-def test_cube_one_pass(ctx):
+def test_cube_one_pass(ctx, monkeypatch):
+    # the general one-pass form on a cube (INCA_MIXED otherwise takes the separable form there)
+    monkeypatch.setenv("INCA_CUBE_SEPARABLE", "0")
     ctx.grid_cube([0.0, 0.0, 0.0], [0.15, 0.15, 0.15], [32, 32, 32])
     ref = ctx.eval(mode=0)
     I = ctx.eval(mode=1, tol=1e-8)
@@ -91,7 +93,8 @@ def test_cube_one_pass(ctx):
 
 
 @pytest.mark.parametrize("grid", ["scan", "cube", "small"])
-def test_graph_replay_matches_eager(ctx, grid):
+def test_graph_replay_matches_eager(ctx, grid, monkeypatch):
+    monkeypatch.setenv("INCA_CUBE_SEPARABLE", "0")  # the cube case captures the general form
     if grid == "scan":
         ctx.grid_scan(*SCAN)
     elif grid == "cube":
