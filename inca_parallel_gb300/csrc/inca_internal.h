@@ -201,6 +201,7 @@ struct inca_ctx {
   // grid changes)
   inca::DevBuf<double> d_cube_axes;
   int64_t cube_axes_version = -1;
+  float cube_floor_log2 = -120.0f;  // record floor of the last separable evaluation
 
   // scratch
   inca::DevBuf<double> d_partial;
@@ -249,7 +250,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc, int* stride, dou
 int ensure_exp_table(inca_ctx* c);
 // cube_eval.cu
 bool cube_separable(const inca_ctx* c);
-int eval_cube_separable(inca_ctx* c);
+int eval_cube_separable(inca_ctx* c, double eps);
 
 // grid_build.cu
 int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,

@@ -1792,7 +1792,7 @@ int ensure_exp_table(inca_ctx* c) {
 }
 
 int eval_mixed(inca_ctx* c, double eps) {
-  if (cube_separable(c)) return eval_cube_separable(c);  // cube lattices: cube_eval.cu
+  if (cube_separable(c)) return eval_cube_separable(c, eps);  // cube lattices: cube_eval.cu
   if (c->chunks.empty()) {
     INCA_CUDA(c, cudaMemsetAsync(c->d_ivec.p, 0, sizeof(double) * c->ngrid, c->stream));
     INCA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1888,7 +1888,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
 }
 
 int eval_mixed_graph(inca_ctx* c, double eps) {
-  if (cube_separable(c)) return eval_cube_separable(c);  // two launches, no planning: run directly
+  if (cube_separable(c)) return eval_cube_separable(c, eps);  // a few launches: run directly
   if (c->chunks.empty()) return eval_mixed(c, eps);
   const void* bufs[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};
   const bool fresh = c->graph_exec && c->graph_grid == c->grid_version && c->graph_prep == c->prepare_count &&
