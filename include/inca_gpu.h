@@ -131,8 +131,8 @@ int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* c
  * outputs (ignored for INCA_FP64; <= 0 selects 1e-10). ivec (ngrid) may be NULL (result
  * stays on the device for the reductions). On a cube lattice (inca_grid_cube, one molecule)
  * INCA_MIXED evaluates the lattice's separable factors in double-float (about 2^-44 relative
- * per term, whatever tol asks for); the environment variable INCA_CUBE_SEPARABLE=0 selects the
- * general mixed form there instead. */
+ * per term) and leaves out only quartets whose terms sum to at most 5% of tol times max|I|;
+ * the environment variable INCA_CUBE_SEPARABLE=0 selects the general mixed form there instead. */
 int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 
 /* Schedule of the mixed evaluation: work items per resident CTA of the persistent passes,
