@@ -79,6 +79,12 @@ constexpr double kDropFrac = 0.05;
 constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kFold = 8;                 // chunks between FP64 folds
 constexpr int kItemsPerCta = 12;         // persistent passes: work items per resident CTA
+// Records whose |u_d| stays below kFastU over a tile (so y >= -3 kFastU^2 > -1000 and the
+// polynomials cannot overflow) and whose scale ks <= 100 take the term code without clamps.
+#ifndef INCA_FAST_TERMS
+#define INCA_FAST_TERMS 1
+#endif
+constexpr float kFastU = 18.0f;
 // Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
 // whether inline corrections evaluate two terms per lane and round.
 #ifndef INCA_PASS_CTAS_PER_SM
@@ -125,15 +131,19 @@ __device__ constexpr float kExp2C[8] = {1.5303699910873547e-05f, 0.0001546972926
 constexpr float kRoundShift = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundShiftBits = 0x4B400000;
 
+// kSafe = false: the caller guarantees y >= -1000 and ks <= 100 (then the clamp of y and the
+// upper clamp of the exponent field change nothing, so both forms give the same bits).
+template <bool kSafe = true>
 __device__ __forceinline__ float exp2_fp32(float y, int ks) {
-  const float yc = fmaxf(y, -1000.0f);
+  const float yc = kSafe ? fmaxf(y, -1000.0f) : y;
   const float t = __fadd_rn(yc, kRoundShift);
   const float n = __fsub_rn(t, kRoundShift);
   const float f = __fsub_rn(yc, n);
   float p = kExp2C[0];
 #pragma unroll
   for (int i = 1; i <= kExp2Deg; ++i) p = __fmaf_rn(p, f, kExp2C[i]);
-  const int e = min(max(__float_as_int(t) + (ks + 127 - kRoundShiftBits), 0), 254);
+  const int eb = max(__float_as_int(t) + (ks + 127 - kRoundShiftBits), 0);
+  const int e = kSafe ? min(eb, 254) : eb;
   return __fmul_rn(p, __int_as_float(e << 23));
 }
 
@@ -174,7 +184,9 @@ __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, con
 //   V_d by Horner (absolute error <= 2 L_d u32 P_d, P_d = sum_k |C_k| |u_d|^k), 4 products
 //   e = u32 |A'| E prod_d P_d (10 + 2 L + 3 |y|).
 // Explicit round-to-nearest intrinsics only, so both passes produce the same bits.
-template <int NP, bool kErr>
+// kSafe = false (records whose |u_d| stays below kFastU over the tile, and ks <= 100): the
+// clamps of u and y are left out; they would change nothing there, so the bits are the same.
+template <int NP, bool kErr, bool kSafe = true>
 __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
                                         const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
 #if INCA_REC_VEC
@@ -208,16 +220,18 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
     y = __fmaf_rn(-u[1][p], u[1][p], y);
     y = __fmaf_rn(-u[2][p], u[2][p], y);
     Y[p] = y;
-    E[p] = exp2_fp32(y, ks);
+    E[p] = exp2_fp32<kSafe>(y, ks);
   }
   // the polynomials see u clamped to +-kUClamp: wherever E is non-zero |u_d| is far below it,
   // and far points (E = 0) cannot overflow the polynomial into inf (0 * inf = NaN)
+  if (kSafe) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d)
-    if (L[d]) {
+    for (int d = 0; d < 3; ++d)
+      if (L[d]) {
 #pragma unroll
-      for (int p = 0; p < NP; ++p) u[d][p] = fminf(fmaxf(u[d][p], -kUClamp), kUClamp);
-    }
+        for (int p = 0; p < NP; ++p) u[d][p] = fminf(fmaxf(u[d][p], -kUClamp), kUClamp);
+      }
+  }
   const float* Cx = R + 12;
   const float* Cy = Cx + L[0] + 1;
   const float* Cz = Cy + L[1] + 1;
@@ -650,8 +664,12 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       const ClassSeg sg = segs[w.cls];
       const float* st = S.buf[k & 1];
       const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
-      const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
+      float umax = HUGE_VALF;
+      const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box, nullptr, &umax) : -HUGE_VALF;
       uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      const uint32_t fast = INCA_FAST_TERMS ? __ballot_sync(0xffffffffu, lane < w.count && umax < kFastU &&
+                                                                           st[lane * sg.stride32 + 11] <= 100.0f)
+                                            : 0u;
       if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
       if (lane == 0) {
         nskip += w.count - __popc(m);
@@ -692,7 +710,10 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         }
 #else
         float t[kPPT], e[kPPT];
-        terms32<kPPT, true>(st + q * sg.stride32, L, rh, rl, t, e);
+        if ((fast >> q) & 1u)
+          terms32<kPPT, true, false>(st + q * sg.stride32, L, rh, rl, t, e);
+        else
+          terms32<kPPT, true, true>(st + q * sg.stride32, L, rh, rl, t, e);
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
           if (kFuse && e[p] > tau[p]) {

@@ -212,11 +212,12 @@ __device__ __forceinline__ f2 df_exp2(f2 y, int ks, const float2* __restrict__ t
 // log2 upper bound of |A'| E prod_d P_d over a box lo[3], hi[3] of points, from an FP32 record
 // (mixed_eval.cu: u = s (r + d), E = 2^(-|u|^2), P_d = sum_k |Cn_dk| |u_d|^k): la + sum_d
 // [L_d log2 max(1, M_d) - m_d^2] with m_d / M_d the smallest / largest |u_d| over the box, widened
-// by a relative and absolute 1e-5; *lerr gets the log2 bound of the FP32 error bound e over the box.
+// by a relative and absolute 1e-5; *lerr gets the log2 bound of the FP32 error bound e over the box
+// and *umax the largest M_d.
 __device__ __forceinline__ float log2_bound(const float* __restrict__ R, const int L[3], const float* box,
-                                           float* lerr = nullptr) {
+                                           float* lerr = nullptr, float* umax = nullptr) {
   float lb = R[10] + 0.02f;
-  float y2 = 0.0f;
+  float y2 = 0.0f, mm = 0.0f;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float s = R[0], b = R[2 + d];
@@ -227,7 +228,9 @@ __device__ __forceinline__ float log2_bound(const float* __restrict__ R, const i
     M = M * (1.0f + 1e-5f) + 1e-5f;
     lb += static_cast<float>(L[d]) * __log2f(fmaxf(M, 1.0f)) - m * m;
     y2 = fmaf(M, M, y2);
+    mm = fmaxf(mm, M);
   }
+  if (umax) *umax = mm;
   if (lerr) *lerr = lb - 24.0f + __log2f(static_cast<float>(10 + 2 * (L[0] + L[1] + L[2])) + 3.0f * y2) + 0.02f;
   return lb;
 }
