@@ -165,7 +165,7 @@ k_cube_sep(const WorkChunk* __restrict__ chunks, int nchunks, const ClassSeg* __
       if (!ok) break;
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
-      const float* st = S.buf[k & 1];
+      const float* st = S.buf(k);
       const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
       const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box) : -HUGE_VALF;
       uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > floor_log2);

@@ -148,9 +148,35 @@ __device__ __forceinline__ float exp2_fp32(float y, int ks) {
 }
 
 // ---------------------------------------------------------------- FP32 term (both passes)
+// INCA_MERGED_POLY: each dimension's value polynomial and its absolute-coefficient bound share
+// one Horner loop (one coefficient load and one branch per dimension instead of two); the
+// operations and their order are those of the separate loops, so the bits are the same.
+#ifndef INCA_MERGED_POLY
+#define INCA_MERGED_POLY 1
+#endif
 // Polynomial of a class-uniform (warp-uniform) degree L at NP points, Horner with FMA; a loop
 // over the degree (not unrolled) keeps the kernel's code small enough for the instruction cache.
 // kAbs: sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error.
+// poly2_pts: both at once (kErr), or the value alone.
+template <int NP, bool kErr>
+__device__ __forceinline__ void poly2_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP],
+                                          float (&a)[NP]) {
+  const float c0 = C[0];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    v[p] = c0;
+    if (kErr) a[p] = fabsf(c0);
+  }
+#pragma unroll 1
+  for (int m = 1; m <= L; ++m) {
+    const float c = C[m];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      v[p] = __fmaf_rn(v[p], u[p], c);
+      if (kErr) a[p] = __fmaf_rn(a[p], fabsf(u[p]), fabsf(c));
+    }
+  }
+}
 template <int NP, bool kAbs>
 __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
   const float c0 = kAbs ? fabsf(C[0]) : C[0];
@@ -240,6 +266,32 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
 #pragma unroll
   for (int p = 0; p < NP; ++p) P[p] = E[p];
   float v[NP];
+#if INCA_MERGED_POLY
+  float Pe[NP], a[NP];
+  if (kErr) {
+    const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
+    const float aA = 5.9604645e-08f * fabsf(A_hi);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) Pe[p] = __fmul_rn(E[p], __fmaf_rn(fabsf(Y[p]), 3.0f * aA, k0 * fabsf(A_hi)));
+  }
+  const float* Cd[3] = {Cx, Cy, Cz};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) {
+      poly2_pts<NP, kErr>(L[d], Cd[d], u[d], v, a);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        P[p] = __fmul_rn(P[p], v[p]);
+        if (kErr) Pe[p] = __fmul_rn(Pe[p], a[p]);
+      }
+    }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(P[p], A_hi, __fmul_rn(P[p], A_lo));
+  if (kErr) {
+#pragma unroll
+    for (int p = 0; p < NP; ++p) err[p] = Pe[p];
+  }
+#else
   if (L[0]) {
     poly_pts<NP, false>(L[0], Cx, u[0], v);
 #pragma unroll
@@ -280,6 +332,7 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
 #pragma unroll
     for (int p = 0; p < NP; ++p) err[p] = P[p];
   }
+#endif
 }
 
 // ---- packed pairs of FP32 values (two points per instruction: add/sub/mul/fma .f32x2, each
@@ -662,7 +715,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       if (!ok) break;
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
-      const float* st = S.buf[k & 1];
+      const float* st = S.buf(k);
       const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
       float umax = HUGE_VALF;
       const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box, nullptr, &umax) : -HUGE_VALF;
@@ -915,7 +968,7 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       if (!ok) break;
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
-      const float* st = S.buf[k & 1];
+      const float* st = S.buf(k);
       const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
       const float* Rq = st + lane * sg.stride32;
       // the skip decision of the pass over all terms (same box, arithmetic and threshold)

@@ -70,15 +70,19 @@ __device__ __forceinline__ ChunkRef chunk_ref(const WorkChunk* chunks, const Cla
 
 // Shared-memory stage of a warp-CTA (dynamic shared memory): two barriers, then two chunk
 // buffers of `floats` floats each (32 records of the largest stride present).
+// Buffer k & 1 is addressed by arithmetic on the shared-memory base (not by indexing an array of
+// pointers, which the compiler keeps in local memory): the record reads stay shared-memory loads.
 struct Stage {
   uint64_t* bar;
-  float* buf[2];
+  float* buf0;
+  int floats;
+  __device__ __forceinline__ float* buf(int k) const { return buf0 + (k & 1) * floats; }
 };
 __device__ __forceinline__ Stage stage_view(unsigned char* dsm, int floats) {
   Stage S;
   S.bar = reinterpret_cast<uint64_t*>(dsm);
-  S.buf[0] = reinterpret_cast<float*>(dsm + 128);
-  S.buf[1] = S.buf[0] + floats;
+  S.buf0 = reinterpret_cast<float*>(dsm + 128);
+  S.floats = floats;
   return S;
 }
 
@@ -98,7 +102,7 @@ __device__ __forceinline__ void stage_first(const Stage& S, const WorkChunk* chu
   if (threadIdx.x == 0) {
     fence_proxy_async();  // earlier generic-proxy reads of that buffer are done (warp-synchronous)
     const ChunkRef r = chunk_ref(chunks, segs, rec32, ch);
-    bulk_load(S.buf[k & 1], r.src, r.bytes, &S.bar[k & 1]);
+    bulk_load(S.buf(k), r.src, r.bytes, &S.bar[k & 1]);
   }
 }
 
@@ -144,7 +148,7 @@ __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chun
   if (threadIdx.x == 0 && next < nchunks) {
     fence_proxy_async();  // the generic-proxy reads of that buffer (chunk k-1) are done
     const ChunkRef r = chunk_ref(chunks, segs, rec32, next);
-    bulk_load(S.buf[(k + 1) & 1], r.src, r.bytes, &S.bar[(k + 1) & 1]);
+    bulk_load(S.buf(k + 1), r.src, r.bytes, &S.bar[(k + 1) & 1]);
   }
   if (mbar_wait(&S.bar[k & 1], static_cast<uint32_t>((k >> 1) & 1))) return true;
   if (next < nchunks) mbar_wait(&S.bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1));
