@@ -80,3 +80,21 @@ def test_batch_errors(ctx, molecules):
     ctx.grid_scan(*SCAN)  # replaces the batch grid
     with pytest.raises(IncaError, match="INCA_E_STATE"):
         ctx.batch_eval(mode=0)
+
+
+def test_waves_match_one_batch(ctx, molecules):
+    from inca_parallel_gb300 import batch_waves as BW
+    ctx.batch_clear()
+    for b, D in molecules:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN)
+    ctx.batch_prepare(THRESH)
+    ref64 = ctx.batch_eval(mode=0)
+    sizes = [BW.records(len(b["alpha"]), unique=False) for b, _ in molecules]
+    budget = max(sizes)
+    assert len(BW.plan_waves([len(b["alpha"]) for b, _ in molecules], budget, unique=False)) >= 3
+    I64, info = BW.run_waves(ctx, molecules, SCAN, THRESH, 0, 1e-8, max_records=budget, unique=False)
+    assert len(info) >= 3 and sorted(i for w in info for i in w["molecules"]) == list(range(len(molecules)))
+    Im, _ = BW.run_waves(ctx, molecules, SCAN, THRESH, 1, 1e-8, max_records=budget, unique=False)
+    for a, m, r in zip(I64, Im, ref64):
+        np.testing.assert_allclose(a, r, rtol=1e-12, atol=0)
+        assert np.max(np.abs(m - r) / np.abs(r)) <= 1e-8
