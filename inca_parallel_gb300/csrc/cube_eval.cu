@@ -74,13 +74,15 @@ __global__ void k_absmax(int64_t n, const double* __restrict__ x, double* M) {
   if (threadIdx.x == 0) *M = sh[0];
 }
 
-double env_drop_fraction() {
+// The share of the tolerance given to left-out terms: INCA_DROP_FRACTION, else the context's
+// schedule (inca_set_tuning), else 0.05.
+double drop_fraction(const inca_ctx* c) {
   if (const char* e = std::getenv("INCA_DROP_FRACTION")) {
     char* end = nullptr;
     const double v = std::strtod(e, &end);
     if (end != e && v >= 0.0 && v < 0.5) return v;
   }
-  return 0.05;
+  return c->tune_drop >= 0.0 ? c->tune_drop : 0.05;
 }
 
 // Compensated product x y of double-float values, added to the double-float accumulator (h, l):
@@ -394,7 +396,7 @@ int eval_cube_separable(inca_ctx* c, double eps) {
   INCA_CUDA(c, cudaEventRecord(ev[0], c->stream));
   CubeRun run;
   float floor_log2 = kCubeSkipLog2;
-  const double frac = env_drop_fraction();
+  const double frac = drop_fraction(c);
   if (coarse && frac > 0.0 && eps > 0.0) {
     double* sub = c->d_cube_axes.p + naxes;
     INCA_LAUNCH(c, k_cube_axes, static_cast<unsigned>((maxes + 127) / 128), 128, 0, c->d_px.p, c->d_py.p, c->d_pz.p,

@@ -1608,7 +1608,7 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   P.eps = eps;
   // knobs (environment, read per evaluation; tuning and test aids)
   P.tau_scale = env_knob("INCA_TAU_SCALE", kTauScale, 1e-300, HUGE_VAL);
-  P.drop_frac = env_knob("INCA_DROP_FRACTION", kDropFrac, 0.0, 0.5);
+  P.drop_frac = env_knob("INCA_DROP_FRACTION", c->tune_drop >= 0.0 ? c->tune_drop : kDropFrac, 0.0, 0.5);
   P.safety = env_knob("INCA_EST_SAFETY", c->tune_safety >= 0.0 ? c->tune_safety : kEstSafety, 0.0, HUGE_VAL);
   P.nwt = c->ntiles;
   P.ngroups = P.nwt * kPPT;
@@ -1893,27 +1893,32 @@ int eval_mixed(inca_ctx* c, double eps) {
 // records, precision and tolerance plans, runs once eagerly and captures the launch sequence;
 // later calls launch the graph (all host decisions made at planning; the one that depends on
 // the data -- repeating without dropping -- is taken after the replay, eagerly).
-// Schedule tuning by coordinate descent over (items per CTA, sample stride, estimate safety):
-// every candidate is a complete mixed evaluation on the current grid and records, timed with
-// CUDA events (median of `reps` after one untimed run); a candidate replaces the best only when
-// it is at least 1% faster, so timing noise does not move the choice. The fastest stays in the
-// context. All candidates meet the tolerance, so the choice changes only the time. On an error
-// the context's previous schedule is restored.
+// Schedule tuning by coordinate descent over (items per CTA, sample stride, estimate safety,
+// drop fraction): every candidate is a complete mixed evaluation on the current grid and
+// records, timed with CUDA events (median of `reps` after one untimed run); a candidate replaces
+// the best only when it is at least 1% faster, so timing noise does not move the choice. The
+// fastest stays in the context. All candidates meet the tolerance, so the choice changes only
+// the time. On an error the context's previous schedule is restored.
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_out, double* safety_out,
-                   double* best_ms, double* default_ms) {
-  const int saved_ipc = c->tune_items_per_cta, saved_stride = c->tune_sample_stride;
-  const double saved_safety = c->tune_safety;
-  auto timed = [&](int ipc, int stride, double safety, double* ms) -> int {
-    c->tune_items_per_cta = ipc;
-    c->tune_sample_stride = stride;
-    c->tune_safety = safety;
+                   double* drop_out, double* best_ms, double* default_ms) {
+  struct Sched {
+    int ipc, stride;
+    double safety, drop;
+  };
+  const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop};
+  auto apply = [&](const Sched& s) {
+    c->tune_items_per_cta = s.ipc;
+    c->tune_sample_stride = s.stride;
+    c->tune_safety = s.safety;
+    c->tune_drop = s.drop;
+  };
+  auto timed = [&](const Sched& s, double* ms) -> int {
+    apply(s);
     std::vector<double> t;
     for (int r = 0; r < reps + 1; ++r) {
       const int st = eval_mixed(c, eps);
       if (st) {
-        c->tune_items_per_cta = saved_ipc;
-        c->tune_sample_stride = saved_stride;
-        c->tune_safety = saved_safety;
+        apply(saved);
         return st;
       }
       if (r) t.push_back(c->t_total_ms);
@@ -1922,41 +1927,40 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     *ms = t[t.size() / 2];
     return INCA_OK;
   };
-  int ipc = kItemsPerCta, stride = static_cast<int>(kSampleStride);
-  double safety = kEstSafety, best = 0.0;
-  int st = timed(ipc, stride, safety, &best);
+  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac};
+  double best = 0.0;
+  int st = timed(cur, &best);
   if (st) return st;
   *default_ms = best;
   const int ipcs[] = {4, 8, 12, 24, 48};
   const int strides[] = {8, 16, 32};
   const double safeties[] = {0.3, 0.5, 0.7};
-  auto better = [&](double ms) { return ms < 0.99 * best; };
+  const double drops[] = {0.02, 0.05, 0.1, 0.2};
+  auto consider = [&](Sched s) -> int {
+    double ms;
+    const int e = timed(s, &ms);
+    if (e) return e;
+    if (ms < 0.99 * best) {
+      best = ms;
+      cur = s;
+    }
+    return INCA_OK;
+  };
   for (int pass = 0; pass < 2; ++pass) {
-    for (int v : ipcs) {
-      if (v == ipc) continue;
-      double ms;
-      if ((st = timed(v, stride, safety, &ms))) return st;
-      if (better(ms)) { best = ms; ipc = v; }
-    }
-    for (int v : strides) {
-      if (v == stride) continue;
-      double ms;
-      if ((st = timed(ipc, v, safety, &ms))) return st;
-      if (better(ms)) { best = ms; stride = v; }
-    }
-    for (double v : safeties) {
-      if (v == safety) continue;
-      double ms;
-      if ((st = timed(ipc, stride, v, &ms))) return st;
-      if (better(ms)) { best = ms; safety = v; }
-    }
+    for (int v : ipcs)
+      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop}))) return st;
+    for (int v : strides)
+      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop}))) return st;
+    for (double v : safeties)
+      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop}))) return st;
+    for (double v : drops)
+      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v}))) return st;
   }
-  c->tune_items_per_cta = ipc;
-  c->tune_sample_stride = stride;
-  c->tune_safety = safety;
-  *ipc_out = ipc;
-  *stride_out = stride;
-  *safety_out = safety;
+  apply(cur);
+  *ipc_out = cur.ipc;
+  *stride_out = cur.stride;
+  *safety_out = cur.safety;
+  *drop_out = cur.drop;
   *best_ms = best;
   return INCA_OK;
 }
