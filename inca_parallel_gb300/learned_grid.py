@@ -247,6 +247,93 @@ def judge(lg, cases, nrad=50, nang=302, dense=(150, 974), nohydro=True, ctx=None
     return out
 
 
+MULTS = (0.5, 0.7, 1.0, 1.4, 2.0)
+
+
+def centre_components(ctx, cent, Ps, scale, nrad, nang, tol=1e-12):
+    """Each centre's TFVC component of the radial integral (inca_radial_integral's per-centre
+    values) on the multicentre grid with the given per-centre scales and node counts."""
+    nq = len(Ps)
+    ctx.grid_radial(np.broadcast_to(nrad, (nq,)).astype(np.int32), np.broadcast_to(nang, (nq,)).astype(np.int32),
+                    np.asarray(scale, dtype=np.float64), cent, Ps)
+    ctx.eval(mode=1, tol=tol)
+    tot, _, pc, _ = ctx.radial_integral()
+    return tot, pc, ctx.ngrid
+
+
+def targets_3d(ctx, cent, Ps, alf, nrad, nang=302, dense=(150, 974), mults=MULTS, ref=None):
+    """Per centre: log of the multiplier of autogrid's scale (from mults) whose grid gives the
+    centre's TFVC component of the radial integral closest to the dense grid's. The partition
+    weight of a point depends on the centres and Ps, not on the scales, so a centre's component
+    changes only with its own scale and one grid per multiplier serves every centre."""
+    if ref is None:
+        ref = centre_components(ctx, cent, Ps, alf, dense[0], dense[1])[1]
+    errs = np.array([np.abs(centre_components(ctx, cent, Ps, alf * m, nrad, nang)[1] - ref) for m in mults])
+    return np.log(np.asarray(mults)[np.argmin(errs, axis=0)]), errs
+
+
+def _judge_molecule(rng, natoms_range=(2, 7), nprim_range=(10, 36)):
+    """A seeded molecule with s and p primitives of exponents up to 50 (where the reference's
+    polynomial fit is exact) and its closed-shell 1-RDM."""
+    from . import workloads as W
+    b = W.random_molecule(rng, int(rng.integers(*natoms_range)), int(rng.integers(*nprim_range)))
+    keep = (b["tmn"].sum(1) <= 1) & (b["alpha"] <= 50.0)
+    b = {**b, "alpha": b["alpha"][keep], "tmn": b["tmn"][keep], "xyz": b["xyz"][keep]}
+    nocc = max(1, min(W.electrons(b) // 2, len(b["alpha"]) // 3))
+    D, _ = W.closed_shell_density(b, nocc, int(rng.integers(1 << 30)))
+    return b, D
+
+
+def training_set_3d(ctx, nmol=60, seed=20261208, nrad_set=(30, 50), nang=302):
+    """Features and targets from per-centre dense-grid errors: the scale column from
+    targets_3d, the node-count column from the 1D rule (targets). Molecules with real DM2s
+    (generated on the device), evaluated by the engine."""
+    from . import centercalc
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    for _ in range(nmol):
+        b, D = _judge_molecule(rng)
+        ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+        ctx.gen_closed_shell_dm2(D, unique=True)
+        ctx.prepare(1e-12)
+        cent, Ps, alf = centercalc(b["an"], b["cartes"])
+        ref = centre_components(ctx, cent, Ps, alf, 150, 974)[1]
+        for nrad in nrad_set:
+            F, E = features(b, cent, Ps, alf, nrad)
+            t3, _ = targets_3d(ctx, cent, Ps, alf, nrad, nang, ref=ref)
+            X.append(F)
+            Y.append(np.stack([t3, targets(E, alf, nrad)[:, 1]], axis=1))
+    return np.vstack(X), np.vstack(Y)
+
+
+def judge_equal_points(lg, cases, nrads=(30, 50), nang=302, dense=(150, 974), ctx=None):
+    """Per case and nrad: the radial-integral error against the dense grid with autogrid's scales
+    and with the learned scales, both with nrad nodes on every centre (equal points)."""
+    from . import Context, centercalc
+    own = ctx is None
+    ctx = ctx or Context(0)
+    out = []
+    try:
+        for b, D in cases:
+            ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+            ctx.gen_closed_shell_dm2(D, unique=True)
+            ctx.prepare(1e-12)
+            cent, Ps, alf = centercalc(b["an"], b["cartes"])
+            ref = centre_components(ctx, cent, Ps, alf, dense[0], dense[1])[0]
+            row = {"centres": len(Ps)}
+            for nrad in nrads:
+                _, _, scale, _, ok = lg.grid(b, nrad)
+                auto, _, na = centre_components(ctx, cent, Ps, alf, nrad, nang)
+                mine, _, nm = centre_components(ctx, cent, Ps, scale, nrad, nang)
+                row[nrad] = {"auto_err": abs(auto - ref) / abs(ref), "learned_err": abs(mine - ref) / abs(ref),
+                             "points": [na, nm], "predicted": int(ok.sum())}
+            out.append(row)
+    finally:
+        if own:
+            ctx.close()
+    return out
+
+
 def main(argv=None):
     """Train on autogrid's centres for 500 seeded geometries of 2-20 atoms and judge the learned
     grids against dense grids (nrad 150, nang 974) on held-out molecules with real DM2s:

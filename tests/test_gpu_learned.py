@@ -78,3 +78,22 @@ def test_predictor_gains_on_held_out_molecules():
     print("held-out centres", len(lr), "mean log10 ratio", lr.mean(), "improved", (lr < 0).mean(), "fallbacks", fallbacks)
     assert lr.mean() < -0.3, lr.mean()
     assert (lr < 0).mean() >= 0.5
+
+
+def test_per_centre_dense_grid_targets():
+    # targets from the TFVC components of the radial integral against a dense grid: one grid per
+    # multiplier serves every centre, and each centre's target is its own best multiplier
+    from inca_parallel_gb300 import Context, centercalc
+    rng = np.random.default_rng(12)
+    b, D = LG._judge_molecule(rng, natoms_range=(3, 4), nprim_range=(12, 16))
+    with Context(0) as ctx:
+        ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+        ctx.gen_closed_shell_dm2(D, unique=True)
+        ctx.prepare(1e-12)
+        cent, Ps, alf = centercalc(b["an"], b["cartes"])
+        tot, pc, _ = LG.centre_components(ctx, cent, Ps, alf, 40, 194)
+        assert abs(pc.sum() - tot) <= 1e-12 * abs(tot)
+        t3, errs = LG.targets_3d(ctx, cent, Ps, alf, 30, 194, dense=(80, 434))
+        assert errs.shape == (len(LG.MULTS), len(Ps))
+        best = np.log(np.asarray(LG.MULTS))[np.argmin(errs, axis=0)]
+        np.testing.assert_array_equal(t3, best)
