@@ -93,41 +93,23 @@ constexpr float kFastU = 18.0f;
 #ifndef INCA_DF_PAIRS
 #define INCA_DF_PAIRS 1
 #endif
-// coefficient prefetch in the Horner loops of the pass-1 term evaluation
-#ifndef INCA_POLY_PF
-#define INCA_POLY_PF 0
-#endif
-// 16-byte loads of the record head in the pass-1 term evaluation
-#ifndef INCA_REC_VEC
-#define INCA_REC_VEC 1
-#endif
 
 // 2^y for y <= 0 in FP32 without systematic bias: y = n + f (n = rint(y), |f| <= 1/2),
 // 2^f by a polynomial evaluated by FMA Horner, times 2^(n + ks) built from the exponent bits
 // (exact; 0 below 2^-126). ks: an integer power of two applied exactly in the final scaling.
 // Polynomials (coefficients highest degree first, FP32): degree 6, minimax relative
 // approximation of 2^x on [-1/2, 1/2] (1.9e-9; with the FP32 Horner steps 7.9e-8 = 1.32 u32
-// measured over 2e6 points, mean 2.6e-10); degree 7 (INCA_EXP2_DEG=7), Chebyshev interpolation
-// (3.2e-9; 6.8e-8 = 1.13 u32 with Horner). The error bound of a term allows 2 u32 for E. The
+// measured over 2e6 points, mean 2.6e-10; a degree-7 Chebyshev interpolant, 3.2e-9 and 1.13
+// u32 with Horner, was measured 3 % slower in the kernel). The error bound of a term allows 2 u32 for E. The
 // hardware ex2.approx was measured biased by -5e-8 relative on this range, which the error
 // model of the correction pass cannot absorb.
 // Rounding: y is clamped to [-1000, 0] (below -1000 the scale is zero for every ks used here)
 // and t = y + 1.5 * 2^23 rounds it to an integer in the low mantissa bits (ties to even, as
 // rint), so n = t - 1.5 * 2^23 and f = y - n are exact and the exponent field is the integer
 // bits of t plus a per-record constant: no conversion instructions.
-#ifndef INCA_EXP2_DEG
-#define INCA_EXP2_DEG 6
-#endif
-#if INCA_EXP2_DEG == 6
 constexpr int kExp2Deg = 6;
 __device__ constexpr float kExp2C[7] = {1.534581242594868e-4f, 1.3399930903688073e-3f, 9.618489071726799e-3f,
                                         5.550328642129898e-2f, 0.24022646248340607f, 0.6931471824645996f, 1.0f};
-#else
-constexpr int kExp2Deg = 7;
-__device__ constexpr float kExp2C[8] = {1.5303699910873547e-05f, 0.00015469729260075837f, 0.0013333478709682822f,
-                                        0.00961802527308464f,    0.05550410971045494f,    0.24022650718688965f,
-                                        0.6931471824645996f,     1.0f};
-#endif
 constexpr float kRoundShift = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundShiftBits = 0x4B400000;
 
@@ -148,16 +130,12 @@ __device__ __forceinline__ float exp2_fp32(float y, int ks) {
 }
 
 // ---------------------------------------------------------------- FP32 term (both passes)
-// INCA_MERGED_POLY: each dimension's value polynomial and its absolute-coefficient bound share
-// one Horner loop (one coefficient load and one branch per dimension instead of two); the
-// operations and their order are those of the separate loops, so the bits are the same.
-#ifndef INCA_MERGED_POLY
-#define INCA_MERGED_POLY 1
-#endif
-// Polynomial of a class-uniform (warp-uniform) degree L at NP points, Horner with FMA; a loop
+// Each dimension's value polynomial and its absolute-coefficient bound share one Horner loop
+// (one coefficient load and one branch per dimension; as two separate loops the kernel took
+// 12 % longer, with the same bits): poly2_pts evaluates a polynomial of a class-uniform
+// (warp-uniform) degree L at NP points by Horner with FMA and, with kErr, the bound
+// sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error. A loop
 // over the degree (not unrolled) keeps the kernel's code small enough for the instruction cache.
-// kAbs: sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error.
-// poly2_pts: both at once (kErr), or the value alone.
 template <int NP, bool kErr>
 __device__ __forceinline__ void poly2_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP],
                                           float (&a)[NP]) {
@@ -177,32 +155,6 @@ __device__ __forceinline__ void poly2_pts(int L, const float* __restrict__ C, co
     }
   }
 }
-template <int NP, bool kAbs>
-__device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP]) {
-  const float c0 = kAbs ? fabsf(C[0]) : C[0];
-#pragma unroll
-  for (int p = 0; p < NP; ++p) v[p] = c0;
-#if INCA_POLY_PF
-  // the next coefficient is loaded one step ahead (C[L + 1] is still inside the record: the
-  // coefficient lists are followed by their low parts)
-  float c = C[1];
-#pragma unroll 1
-  for (int m = 1; m <= L; ++m) {
-    const float cn = C[m + 1];
-    const float ca = kAbs ? fabsf(c) : c;
-#pragma unroll
-    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], kAbs ? fabsf(u[p]) : u[p], ca);
-    c = cn;
-  }
-#else
-#pragma unroll 1
-  for (int m = 1; m <= L; ++m) {
-    const float c = kAbs ? fabsf(C[m]) : C[m];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) v[p] = __fmaf_rn(v[p], kAbs ? fabsf(u[p]) : u[p], c);
-  }
-#endif
-}
 
 // The FP32 term of quartet record R at NP points, and a bound e on its rounding error:
 //   u_d = fma(s_hi, r_hi, b_hi) + [s_hi r_lo + s_lo r_hi + b_lo]  (error <= u32 |u_d|)
@@ -215,7 +167,6 @@ __device__ __forceinline__ void poly_pts(int L, const float* __restrict__ C, con
 template <int NP, bool kErr, bool kSafe = true>
 __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
                                         const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
-#if INCA_REC_VEC
   // the record head in three 16-byte loads (records are 16-byte aligned: strides of 4 floats)
   const float4 R0 = *reinterpret_cast<const float4*>(R);
   const float4 R1 = *reinterpret_cast<const float4*>(R + 4);
@@ -223,11 +174,6 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
   const float s_hi = R0.x, s_lo = R0.y, A_hi = R2.x, A_lo = R2.y;
   const int ks = static_cast<int>(R2.w);
   const float bh[3] = {R0.z, R0.w, R1.x}, bl[3] = {R1.y, R1.z, R1.w};
-#else
-  const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
-  const int ks = static_cast<int>(R[11]);
-  const float bh[3] = {R[2], R[3], R[4]}, bl[3] = {R[5], R[6], R[7]};
-#endif
   float u[3][NP];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -266,7 +212,6 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
 #pragma unroll
   for (int p = 0; p < NP; ++p) P[p] = E[p];
   float v[NP];
-#if INCA_MERGED_POLY
   float Pe[NP], a[NP];
   if (kErr) {
     const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
@@ -290,185 +235,6 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
   if (kErr) {
 #pragma unroll
     for (int p = 0; p < NP; ++p) err[p] = Pe[p];
-  }
-#else
-  if (L[0]) {
-    poly_pts<NP, false>(L[0], Cx, u[0], v);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-  }
-  if (L[1]) {
-    poly_pts<NP, false>(L[1], Cy, u[1], v);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-  }
-  if (L[2]) {
-    poly_pts<NP, false>(L[2], Cz, u[2], v);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-  }
-#pragma unroll
-  for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(P[p], A_hi, __fmul_rn(P[p], A_lo));
-  if (kErr) {
-    const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
-    const float aA = 5.9604645e-08f * fabsf(A_hi);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(E[p], __fmaf_rn(fabsf(Y[p]), 3.0f * aA, k0 * fabsf(A_hi)));
-    if (L[0]) {
-      poly_pts<NP, true>(L[0], Cx, u[0], v);
-#pragma unroll
-      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-    }
-    if (L[1]) {
-      poly_pts<NP, true>(L[1], Cy, u[1], v);
-#pragma unroll
-      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-    }
-    if (L[2]) {
-      poly_pts<NP, true>(L[2], Cz, u[2], v);
-#pragma unroll
-      for (int p = 0; p < NP; ++p) P[p] = __fmul_rn(P[p], v[p]);
-    }
-#pragma unroll
-    for (int p = 0; p < NP; ++p) err[p] = P[p];
-  }
-#endif
-}
-
-// ---- packed pairs of FP32 values (two points per instruction: add/sub/mul/fma .f32x2, each
-// half rounded exactly as the scalar instruction). Off by default: on the bench workload the
-// packed pass-1 kernel gives bit-identical sums but runs 9 % slower (the per-element steps --
-// rounding, exponent bits, clamps, correction tests -- add register moves).
-#ifndef INCA_F32X2
-#define INCA_F32X2 0
-#endif
-struct P2 {
-  unsigned long long v;
-};
-__device__ __forceinline__ P2 pk(float a, float b) {
-  P2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ P2 pb(float a) { return pk(a, a); }
-__device__ __forceinline__ void up(P2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v)); }
-__device__ __forceinline__ P2 padd(P2 a, P2 b) {
-  P2 r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
-  return r;
-}
-__device__ __forceinline__ P2 psub(P2 a, P2 b) {
-  P2 r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
-  return r;
-}
-__device__ __forceinline__ P2 pmul(P2 a, P2 b) {
-  P2 r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
-  return r;
-}
-__device__ __forceinline__ P2 pfma(P2 a, P2 b, P2 c) {
-  P2 r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
-  return r;
-}
-__device__ __forceinline__ P2 pabs(P2 a) {
-  float x, y;
-  up(a, x, y);
-  return pk(fabsf(x), fabsf(y));
-}
-
-// exp2 of y = -q for two values (q >= 0), bit-identical to exp2_fp32(-q, ks) on each: with
-// g = q + n = -(y - n) = -f, the Horner steps in f are evaluated in g with the coefficient of
-// degree k multiplied by (-1)^k, which gives the same roundings (negation is exact and
-// rounding is odd-symmetric) and the same sign at the end (degree 0).
-__device__ __forceinline__ P2 exp2_neg_x2(P2 q, int ks) {
-  float q0, q1;
-  up(q, q0, q1);
-  q0 = fminf(q0, 1000.0f);
-  q1 = fminf(q1, 1000.0f);
-  const float t0 = __fadd_rn(-q0, kRoundShift), t1 = __fadd_rn(-q1, kRoundShift);
-  const P2 g = padd(pk(q0, q1), pk(__fsub_rn(t0, kRoundShift), __fsub_rn(t1, kRoundShift)));
-  P2 p = pb((kExp2Deg & 1) ? -kExp2C[0] : kExp2C[0]);
-#pragma unroll
-  for (int i = 1; i <= kExp2Deg; ++i) p = pfma(p, g, pb(((kExp2Deg - i) & 1) ? -kExp2C[i] : kExp2C[i]));
-  const int e0 = min(max(__float_as_int(t0) + (ks + 127 - kRoundShiftBits), 0), 254);
-  const int e1 = min(max(__float_as_int(t1) + (ks + 127 - kRoundShiftBits), 0), 254);
-  return pmul(p, pk(__int_as_float(e0 << 23), __int_as_float(e1 << 23)));
-}
-
-// Horner of a class-uniform degree for two packed points (loop over the degree).
-template <bool kAbs>
-__device__ __forceinline__ P2 poly_x2(int L, const float* __restrict__ C, P2 u) {
-  P2 v = pb(kAbs ? fabsf(C[0]) : C[0]);
-#pragma unroll 1
-  for (int m = 1; m <= L; ++m) v = pfma(v, u, pb(kAbs ? fabsf(C[m]) : C[m]));
-  return v;
-}
-
-// terms32<4, kErr> with the points in packed pairs (0, 1) and (2, 3): the same operations in the
-// same order, so every term and bound is bit-identical to the scalar form (and to term32_one).
-template <bool kErr>
-__device__ __forceinline__ void terms32_x2(const float* __restrict__ R, const int L[3], const P2 (&rh)[3][2],
-                                           const P2 (&rl)[3][2], P2 (&t)[2], P2 (&err)[2]) {
-  const float s_hi = R[0], s_lo = R[1], A_hi = R[8], A_lo = R[9];
-  const int ks = static_cast<int>(R[11]);
-  P2 u[3][2];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const P2 b_hi = pb(R[2 + d]), b_lo = pb(R[5 + d]);
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      P2 t1 = pfma(pb(s_lo), rh[d][k], b_lo);
-      t1 = pfma(pb(s_hi), rl[d][k], t1);
-      u[d][k] = padd(pfma(pb(s_hi), rh[d][k], b_hi), t1);
-    }
-  }
-  P2 E[2], Q[2];
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    P2 q = pmul(u[0][k], u[0][k]);
-    q = pfma(u[1][k], u[1][k], q);
-    q = pfma(u[2][k], u[2][k], q);
-    Q[k] = q;
-    E[k] = exp2_neg_x2(q, ks);
-  }
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-    if (L[d]) {
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        float a, b;
-        up(u[d][k], a, b);
-        u[d][k] = pk(fminf(fmaxf(a, -kUClamp), kUClamp), fminf(fmaxf(b, -kUClamp), kUClamp));
-      }
-    }
-  const float* Cx = R + 12;
-  const float* Cy = Cx + L[0] + 1;
-  const float* Cz = Cy + L[1] + 1;
-  const float* Cd[3] = {Cx, Cy, Cz};
-  P2 P[2] = {E[0], E[1]};
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-    if (L[d]) {
-#pragma unroll
-      for (int k = 0; k < 2; ++k) P[k] = pmul(P[k], poly_x2<false>(L[d], Cd[d], u[d][k]));
-    }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) t[k] = pfma(P[k], pb(A_hi), pmul(P[k], pb(A_lo)));
-  if (kErr) {
-    const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
-    const float aA = 5.9604645e-08f * fabsf(A_hi);
-#pragma unroll
-    for (int k = 0; k < 2; ++k) P[k] = pmul(E[k], pfma(Q[k], pb(3.0f * aA), pb(k0 * fabsf(A_hi))));
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      if (L[d]) {
-#pragma unroll
-        for (int k = 0; k < 2; ++k) P[k] = pmul(P[k], poly_x2<true>(L[d], Cd[d], pabs(u[d][k])));
-      }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) err[k] = P[k];
   }
 }
 
@@ -659,25 +425,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     }
     const TileInfo T = tiles[wtile];
     if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
-    float rhs[3][kPPT], rls[3][kPPT];
-    load_points(phi, plo, T, lane, rhs, rls);
-#if INCA_F32X2
-    P2 rh[3][2], rl[3][2];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int k2 = 0; k2 < 2; ++k2) {
-        rh[d][k2] = pk(rhs[d][2 * k2], rhs[d][2 * k2 + 1]);
-        rl[d][k2] = pk(rls[d][2 * k2], rls[d][2 * k2 + 1]);
-      }
-#define INCA_RH(d, p) rhs[d][p]
-#define INCA_RL(d, p) rls[d][p]
-#else
-    float (&rh)[3][kPPT] = rhs;
-    float (&rl)[3][kPPT] = rls;
-#define INCA_RH(d, p) rh[d][p]
-#define INCA_RL(d, p) rl[d][p]
-#endif
+    float rh[3][kPPT], rl[3][kPPT];
+    load_points(phi, plo, T, lane, rh, rl);
     float tau[kPPT];
     f2 corr[kPPT];
     if (kFuse) {
@@ -698,15 +447,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     double acc[kPPT];
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) acc[p] = 0.0;
-#if INCA_F32X2
-    P2 sh[2], sl[2], sa[2];
-#pragma unroll
-    for (int k2 = 0; k2 < 2; ++k2) sh[k2] = sl[k2] = sa[k2] = pb(0.0f);
-#else
     float sh[kPPT], sl[kPPT], sa[kPPT];
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) sh[p] = sl[p] = sa[p] = 0.0f;
-#endif
     __syncwarp();
     int nfold = 0;
     bool ok = true;
@@ -734,34 +477,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       while (m) {
         const int q = __ffs(m) - 1;
         m &= m - 1;
-#if INCA_F32X2
-        P2 t2[2], e2[2];
-        terms32_x2<true>(st + q * sg.stride32, L, rh, rl, t2, e2);
-#pragma unroll
-        for (int k2 = 0; k2 < 2; ++k2) {
-          if (kFuse) {
-            float ta, tb, ea, eb;
-            up(t2[k2], ta, tb);
-            up(e2[k2], ea, eb);
-            if (ea > tau[2 * k2]) {
-              nm[2 * k2] |= 1u << q;
-              ta = 0.0f;
-            }
-            if (eb > tau[2 * k2 + 1]) {
-              nm[2 * k2 + 1] |= 1u << q;
-              tb = 0.0f;
-            }
-            t2[k2] = pk(ta, tb);
-          }
-          // TwoSum of the pair sums and the term, packed
-          const P2 s2 = padd(sh[k2], t2[k2]);
-          const P2 bb = psub(s2, sh[k2]);
-          const P2 lo = padd(psub(sh[k2], psub(s2, bb)), psub(t2[k2], bb));
-          sh[k2] = s2;
-          sl[k2] = padd(sl[k2], lo);
-          sa[k2] = padd(sa[k2], e2[k2]);
-        }
-#else
         float t[kPPT], e[kPPT];
         if ((fast >> q) & 1u)
           terms32<kPPT, true, false>(st + q * sg.stride32, L, rh, rl, t, e);
@@ -778,7 +493,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           sl[p] = __fadd_rn(sl[p], s2.lo);
           sa[p] = __fadd_rn(sa[p], e[p]);
         }
-#endif
       }
       if (kFuse) {
 #pragma unroll
@@ -791,8 +505,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
             if (!INCA_DF_PAIRS && mm) {
               const int q = __ffs(mm) - 1;
               mm &= mm - 1;
-              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], INCA_RH(0, p), INCA_RH(1, p),
-                                     INCA_RH(2, p), INCA_RL(0, p), INCA_RL(1, p), INCA_RL(2, p), tab);
+              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p],
+                                     rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
               corr[p] = df_add(corr[p], tdf);
               ++ncorr;
             } else if (mm) {
@@ -802,8 +516,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
               const int qb = two ? __ffs(mm) - 1 : qa;
               if (two) mm &= mm - 1;
               const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2],
-                                      INCA_RH(0, p), INCA_RH(1, p), INCA_RH(2, p), INCA_RL(0, p), INCA_RL(1, p),
-                                      INCA_RL(2, p), tab);
+                                      rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p],
+                                      rl[2][p], tab);
               corr[p] = df_add(corr[p], r.a);
               if (two) corr[p] = df_add(corr[p], r.b);
               ncorr += two ? 2 : 1;
@@ -813,29 +527,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       }
       // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
       const bool fold = ++nfold == kFold;
-#if INCA_F32X2
-#pragma unroll
-      for (int k2 = 0; k2 < 2; ++k2) {
-        const P2 r = padd(sh[k2], sl[k2]);  // fast TwoSum, packed
-        sl[k2] = psub(sl[k2], psub(r, sh[k2]));
-        sh[k2] = r;
-        if (fold) {
-          float h0, h1, l0, l1;
-          up(sh[k2], h0, h1);
-          up(sl[k2], l0, l1);
-          acc[2 * k2] += static_cast<double>(h0) + static_cast<double>(l0);
-          acc[2 * k2 + 1] += static_cast<double>(h1) + static_cast<double>(l1);
-          sh[k2] = sl[k2] = pb(0.0f);
-        }
-      }
-      if (kFuse && fold) {
-#pragma unroll
-        for (int p = 0; p < kPPT; ++p) {
-          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-          corr[p] = {0.0f, 0.0f};
-        }
-      }
-#else
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         const f2 r = fast_two_sum(sh[p], sl[p]);
@@ -850,7 +541,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           }
         }
       }
-#endif
       if (fold) nfold = 0;
       __syncwarp();
     }
@@ -858,21 +548,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       if (lane == 0) atomicExch(err, 1);
       break;
     }
-#if INCA_F32X2
-    float shs[kPPT], sls[kPPT], sas[kPPT];
-#pragma unroll
-    for (int k2 = 0; k2 < 2; ++k2) {
-      up(sh[k2], shs[2 * k2], shs[2 * k2 + 1]);
-      up(sl[k2], sls[2 * k2], sls[2 * k2 + 1]);
-      up(sa[k2], sas[2 * k2], sas[2 * k2 + 1]);
-    }
-#else
     float (&shs)[kPPT] = sh;
     float (&sls)[kPPT] = sl;
     float (&sas)[kPPT] = sa;
-#endif
-#undef INCA_RH
-#undef INCA_RL
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
       acc[p] += static_cast<double>(shs[p]) + static_cast<double>(sls[p]);
