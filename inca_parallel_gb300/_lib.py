@@ -298,8 +298,16 @@ class Context:
         return out
 
     # ---- evaluation / reductions
-    def eval(self, mode=INCA_FP64, tol=1e-10, copy=True):
-        iv = np.zeros(self.ngrid) if copy else None
+    def eval(self, mode=INCA_FP64, tol=1e-10, copy=True, out=None):
+        """I at every grid point (a new array, or `out`: contiguous float64 of ngrid values, e.g.
+        pinned host memory); copy=False leaves the result on the device only."""
+        if out is not None:
+            if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                    and out.size == self.ngrid):
+                raise ValueError("out must be a contiguous float64 array of ngrid values")
+            iv = out
+        else:
+            iv = np.zeros(self.ngrid) if copy else None
         self._check(self.lib.inca_eval(self.h, mode, tol, _d(iv)))
         return iv
 

@@ -160,13 +160,15 @@ int inca_set_primitives(inca_ctx* c, int32_t nprim, const double* alpha, const i
   return INCA_OK;
 }
 
-static int upload_quartets(inca_ctx* c, const std::vector<int4>& ijkl, const std::vector<double>& v) {
-  const int64_t n = static_cast<int64_t>(v.size());
+// ijkl: n records of four 1-based int32 indices, the layout of the device's int4 array, so both
+// arrays go to the device in one copy each straight from the caller's memory (a direct DMA when
+// the caller's buffers are pinned).
+static int upload_quartets(inca_ctx* c, int64_t n, const int32_t* ijkl, const double* v) {
   if (c->d_ijkl.reserve(std::max<int64_t>(n, 1)) || c->d_v.reserve(std::max<int64_t>(n, 1)))
     return set_error(c, INCA_E_NOMEM, "quartets");
   if (n > 0) {
-    INCA_CUDA(c, cudaMemcpyAsync(c->d_ijkl.p, ijkl.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, c->stream));
-    INCA_CUDA(c, cudaMemcpyAsync(c->d_v.p, v.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    INCA_CUDA(c, cudaMemcpyAsync(c->d_ijkl.p, ijkl, sizeof(int4) * n, cudaMemcpyHostToDevice, c->stream));
+    INCA_CUDA(c, cudaMemcpyAsync(c->d_v.p, v, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     INCA_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   c->nq = n;
@@ -185,16 +187,14 @@ int inca_load_dm2p(inca_ctx* c, const char* path, int64_t* nread) {
   const int st = read_dm2p(path, c->nprim, q, v, err);
   if (st) return set_error(c, st, err);
   if (nread) *nread = static_cast<int64_t>(v.size());
-  return upload_quartets(c, q, v);
+  static_assert(sizeof(int4) == 4 * sizeof(int32_t), "int4 holds four int32 indices");
+  return upload_quartets(c, static_cast<int64_t>(v.size()), reinterpret_cast<const int32_t*>(q.data()), v.data());
 }
 
 int inca_set_quartets(inca_ctx* c, int64_t n, const int32_t* ijkl, const double* v) {
   CTX_CHECK(c);
   if (n < 0 || (n > 0 && (!ijkl || !v))) return set_error(c, INCA_E_ARG, "inca_set_quartets: bad arguments");
-  std::vector<int4> q(n);
-  std::vector<double> vv(v, v + n);
-  for (int64_t i = 0; i < n; ++i) q[i] = make_int4(ijkl[4 * i], ijkl[4 * i + 1], ijkl[4 * i + 2], ijkl[4 * i + 3]);
-  return upload_quartets(c, q, vv);
+  return upload_quartets(c, n, ijkl, v);
 }
 
 int inca_gen_closed_shell_dm2(inca_ctx* c, const double* D, int unique, int64_t* nrecords) {
@@ -349,7 +349,10 @@ int inca_eval(inca_ctx* c, int mode, double tol, double* ivec) {
   CTX_CHECK(c);
   const int st = eval_device(c, mode, tol);
   if (st) return st;
-  if (ivec) INCA_CUDA(c, cudaMemcpy(ivec, c->d_ivec.p, sizeof(double) * c->ngrid, cudaMemcpyDeviceToHost));
+  if (ivec) {
+    INCA_CUDA(c, cudaMemcpyAsync(ivec, c->d_ivec.p, sizeof(double) * c->ngrid, cudaMemcpyDeviceToHost, c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
   return INCA_OK;
 }
 
