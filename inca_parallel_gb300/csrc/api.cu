@@ -85,6 +85,7 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_ijkl.release();
   c->d_v.release();
   c->d_flags.release();
+  c->d_ja8.release();
   c->d_s1.release();
   c->d_s2.release();
   c->d_classes.release();

@@ -141,6 +141,7 @@ struct inca_ctx {
   inca_counts counts{0, 0, 0};
   double lim = 0.0;
   inca::DevBuf<uint8_t> d_flags;
+  inca::DevBuf<double> d_ja8;  // JA8 of every primitive pair (screening)
   inca::DevBuf<double> d_s1, d_s2;
   bool have_screen_values = false;
 

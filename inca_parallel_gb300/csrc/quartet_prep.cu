@@ -172,9 +172,28 @@ struct QRec {
   double C[3][kMaxCoef];
 };
 
+// JA8 of every ordered primitive pair (i, k), with the arithmetic of prepare_one (Rik2, aik,
+// eik), so a quartet's screen-1 value reads two table entries instead of evaluating JA8 twice
+// and the values are the same bits.
+__global__ void k_pair_ja8(int nprim, const PrimD* __restrict__ prims, double* __restrict__ J) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(nprim) * nprim) return;
+  const PrimD Pi = prims[t / nprim], Pk = prims[t % nprim];
+  const double aik = Pi.alpha + Pk.alpha;
+  const double eik = (Pi.alpha * Pk.alpha) * (1.0 / aik);
+  const double Xi[3] = {Pi.x, Pi.y, Pi.z}, Xk[3] = {Pk.x, Pk.y, Pk.z};
+  double Rik2 = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) Rik2 = Rik2 + (Xi[d] - Xk[d]) * (Xi[d] - Xk[d]);
+  J[t] = ja8(Pi, Pk, Rik2, aik, eik);
+}
+
+constexpr int kPairTableMax = 4096;
+
 // One quartet (src/mod_intracule.f90:282-343). Returns 0 / 1 (screen 1) / 3 (both).
+// Jtab (optional): the JA8 table of k_pair_ja8.
 __device__ int prepare_one(const PrimD* prims, int4 q, double v, QRec* out, double* s1o,
-                           double* s2o) {
+                           double* s2o, const double* __restrict__ Jtab = nullptr) {
   const PrimD Pi = prims[q.x - 1], Pj = prims[q.y - 1], Pk = prims[q.z - 1], Pl = prims[q.w - 1];
   double DMval = v;
   if (cP.normalize) DMval = v * (((Pi.norm * Pj.norm) * Pk.norm) * Pl.norm);
@@ -189,8 +208,8 @@ __device__ int prepare_one(const PrimD* prims, int4 q, double v, QRec* out, doub
     Rik2 = Rik2 + (Xi[d] - Xk[d]) * (Xi[d] - Xk[d]);
     Rjl2 = Rjl2 + (Xj[d] - Xl[d]) * (Xj[d] - Xl[d]);
   }
-  const double Jik = ja8(Pi, Pk, Rik2, aik, eik);
-  const double Jjl = ja8(Pj, Pl, Rjl2, ajl, ejl);
+  const double Jik = Jtab ? Jtab[static_cast<int64_t>(q.x - 1) * cP.nprim + (q.z - 1)] : ja8(Pi, Pk, Rik2, aik, eik);
+  const double Jjl = Jtab ? Jtab[static_cast<int64_t>(q.y - 1) * cP.nprim + (q.w - 1)] : ja8(Pj, Pl, Rjl2, ajl, ejl);
   const double lim = cP.thresh * Pi.lim_scale;
   const double screen1 = fabs(DMval) * sqrt(Jik * Jjl);
   *s1o = screen1;
@@ -237,17 +256,17 @@ __device__ __forceinline__ uint32_t class_key(const int L[3]) {
 
 __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl, const double* __restrict__ v,
                                        const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
-                                       uint32_t* key, int64_t* idx, int* bad_index);
+                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab);
 
 // Pass 1: screening of every quartet; class key of survivors (others sort last).
 __global__ void k_screen(int64_t n, const int4* __restrict__ ijkl, const double* __restrict__ v,
                          const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
                          uint32_t* key, int64_t* idx, int* bad_index,
-                         unsigned long long* n_screen1) {
+                         unsigned long long* n_screen1, const double* __restrict__ Jtab) {
   const int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const bool live = q < n;
   int f = 0;
-  if (live) f = screen_one(q, ijkl, v, prims, flags, s1, s2, key, idx, bad_index);
+  if (live) f = screen_one(q, ijkl, v, prims, flags, s1, s2, key, idx, bad_index, Jtab);
   // warp-aggregated count of screen-1 survivors
   const unsigned ballot = __ballot_sync(0xffffffffu, live && (f & 1));
   if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(n_screen1, static_cast<unsigned long long>(__popc(ballot)));
@@ -255,7 +274,7 @@ __global__ void k_screen(int64_t n, const int4* __restrict__ ijkl, const double*
 
 __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl, const double* __restrict__ v,
                                        const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
-                                       uint32_t* key, int64_t* idx, int* bad_index) {
+                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab) {
   const int4 r = ijkl[q];
   idx[q] = q;
   if (r.x < 1 || r.y < 1 || r.z < 1 || r.w < 1 || r.x > cP.nprim || r.y > cP.nprim ||
@@ -269,7 +288,7 @@ __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl,
   }
   QRec rec;
   double a1, a2;
-  const int f = prepare_one(prims, r, v[q], &rec, &a1, &a2);
+  const int f = prepare_one(prims, r, v[q], &rec, &a1, &a2, Jtab);
   flags[q] = static_cast<uint8_t>(f);
   if (s1) s1[q] = a1;
   if (s2) s2[q] = a2;
@@ -289,7 +308,8 @@ __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl,
 __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
                         const int4* __restrict__ ijkl, const double* __restrict__ v,
                         const PrimD* __restrict__ prims, const ClassSeg* __restrict__ segs,
-                        int nseg, double* rec64, float* rec32, int64_t* surv_src) {
+                        int nseg, double* rec64, float* rec32, int64_t* surv_src,
+                        const double* __restrict__ Jtab) {
   const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (p >= nsurv) return;
   int lo = 0, hi = nseg - 1;
@@ -302,7 +322,7 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
   surv_src[p] = src;
   QRec rec;
   double a1, a2;
-  prepare_one(prims, ijkl[src], v[src], &rec, &a1, &a2);
+  prepare_one(prims, ijkl[src], v[src], &rec, &a1, &a2, Jtab);
   const int64_t local = p - sg.first;
   double* r64 = rec64 + sg.off64 + local * sg.stride;
   // u-space polynomials: V_d(r') = sum_k C_k r'^k = sum_k (C_k c^-k) u^k, u = c r'
@@ -431,11 +451,23 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   if (e == cudaSuccess) e = cudaMemsetAsync(n1dev.p, 0, sizeof(unsigned long long), c->stream);
   const int bs = 128;
   const int64_t grid = (n + bs - 1) / bs;
+  // JA8 of every primitive pair, once (up to kPairTableMax primitives: 128 MiB); beyond that each
+  // quartet evaluates its two JA8 bounds itself
+  const double* jtab = nullptr;
+  if (e == cudaSuccess && c->nprim <= kPairTableMax) {
+    const int64_t np2 = static_cast<int64_t>(c->nprim) * c->nprim;
+    if (c->d_ja8.reserve(np2) == cudaSuccess) {
+      INCA_LAUNCH(c, k_pair_ja8, static_cast<unsigned>((np2 + 127) / 128), 128, 0, c->nprim, c->d_prims.p,
+                  c->d_ja8.p);
+      e = cudaGetLastError();
+      jtab = c->d_ja8.p;
+    }
+  }
   if (e == cudaSuccess) {
     INCA_LAUNCH(c, k_screen, static_cast<unsigned>(grid), bs, 0, n, c->d_ijkl.p, c->d_v.p, c->d_prims.p, c->d_flags.p,
                                                                 keep_values ? c->d_s1.p : nullptr,
                                                                 keep_values ? c->d_s2.p : nullptr, key.p, idx.p, bad.p,
-                                                                n1dev.p);
+                                                                n1dev.p, jtab);
     e = cudaGetLastError();
   }
   size_t tmp_bytes = 0;
@@ -555,7 +587,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   if (e == cudaSuccess && nsurv > 0) {
     INCA_LAUNCH(c, k_build, static_cast<unsigned>((nsurv + bs - 1) / bs), bs, 0, 
         nsurv, idx2.p, c->d_ijkl.p, c->d_v.p, c->d_prims.p, c->d_classes.p,
-        static_cast<int>(c->classes.size()), c->d_rec64.p, c->d_rec32.p, c->d_surv_src.p);
+        static_cast<int>(c->classes.size()), c->d_rec64.p, c->d_rec32.p, c->d_surv_src.p, jtab);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
