@@ -136,17 +136,18 @@ __device__ __forceinline__ float exp2_fp32(float y, int ks) {
 // (warp-uniform) degree L at NP points by Horner with FMA and, with kErr, the bound
 // sum_k |C_k| |u|^k, which bounds |V(u)| and, times 2 L u32, its Horner rounding error. A loop
 // over the degree (not unrolled) keeps the kernel's code small enough for the instruction cache.
+// L >= 1 (constant polynomials are skipped): the first Horner step starts from C[0] directly.
 template <int NP, bool kErr>
 __device__ __forceinline__ void poly2_pts(int L, const float* __restrict__ C, const float (&u)[NP], float (&v)[NP],
                                           float (&a)[NP]) {
-  const float c0 = C[0];
+  const float c0 = C[0], c1 = C[1];
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
-    v[p] = c0;
-    if (kErr) a[p] = fabsf(c0);
+    v[p] = __fmaf_rn(c0, u[p], c1);
+    if (kErr) a[p] = __fmaf_rn(fabsf(c0), fabsf(u[p]), fabsf(c1));
   }
 #pragma unroll 1
-  for (int m = 1; m <= L; ++m) {
+  for (int m = 2; m <= L; ++m) {
     const float c = C[m];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
