@@ -208,17 +208,14 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
   const float* Cx = R + 12;
   const float* Cy = Cx + L[0] + 1;
   const float* Cz = Cy + L[1] + 1;
-  // dimensions with L_d = 0 have V_d = 1 exactly (sign folded into A'): skipped
-  float P[NP];
-#pragma unroll
-  for (int p = 0; p < NP; ++p) P[p] = E[p];
-  float v[NP];
-  float Pe[NP], a[NP];
+  // dimensions with L_d = 0 have V_d = 1 exactly (sign folded into A'): skipped. E becomes the
+  // product E V_x V_y V_z in place, err its bound.
+  float v[NP], a[NP];
   if (kErr) {
     const float k0 = 5.9604645e-08f * static_cast<float>(10 + 2 * (L[0] + L[1] + L[2]));
     const float aA = 5.9604645e-08f * fabsf(A_hi);
 #pragma unroll
-    for (int p = 0; p < NP; ++p) Pe[p] = __fmul_rn(E[p], __fmaf_rn(fabsf(Y[p]), 3.0f * aA, k0 * fabsf(A_hi)));
+    for (int p = 0; p < NP; ++p) err[p] = __fmul_rn(E[p], __fmaf_rn(fabsf(Y[p]), 3.0f * aA, k0 * fabsf(A_hi)));
   }
   const float* Cd[3] = {Cx, Cy, Cz};
 #pragma unroll
@@ -227,16 +224,12 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
       poly2_pts<NP, kErr>(L[d], Cd[d], u[d], v, a);
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        P[p] = __fmul_rn(P[p], v[p]);
-        if (kErr) Pe[p] = __fmul_rn(Pe[p], a[p]);
+        E[p] = __fmul_rn(E[p], v[p]);
+        if (kErr) err[p] = __fmul_rn(err[p], a[p]);
       }
     }
 #pragma unroll
-  for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(P[p], A_hi, __fmul_rn(P[p], A_lo));
-  if (kErr) {
-#pragma unroll
-    for (int p = 0; p < NP; ++p) err[p] = Pe[p];
-  }
+  for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(E[p], A_hi, __fmul_rn(E[p], A_lo));
 }
 
 // The same FP32 term and error bound for one point with loop-based Horner (compact code for
