@@ -335,6 +335,17 @@ def gpu_arm(args):
             for ln in open(prof):
                 if ln.startswith("traffic_bytes_per_launch:"):
                     traffic = float(ln.split(":")[1])
+        # the two bounds of the contract, for comparison: HBM (traffic of one launch from the ncu
+        # summary over the launch time, against the measured copy bandwidth) and tensor (0: no
+        # contraction on this path)
+        hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+        mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(mp):
+            try:
+                hbm_peak, hbm_src = float(json.load(open(mp))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
+            except (ValueError, KeyError):
+                pass
+        hbm_gbs = traffic / (kms * 1e-3) / 1e9 if traffic else None
         line = {
             "metric": METRIC, "value": value, "unit": "quartet-points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -366,7 +377,11 @@ def gpu_arm(args):
                          "peak_source": "measured: FP32 FMA microkernel (inca_fp32_fma_peak) on this GPU, "
                                         "%.1f TFLOP/s = %.1f T FMA/s" % (fp32_tflops, fp32_tflops / 2.0),
                          "note": "FP32-pipe bound (no contraction, ~0 bytes per quartet-point); "
-                                 "MEASURED_PEAKS.json has no FP32 figure"},
+                                 "MEASURED_PEAKS.json has no FP32 figure",
+                         "hbm_view": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                      "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None, "peak_source": hbm_src},
+                         "tensor_view": {"achieved": 0.0, "unit": "TFLOP/s",
+                                         "note": "sm__pipe_tensor_cycles_active 0 % (ncu)"}},
             "clocks": csum,
             "e2e": {"value": qp / e2e_s, "unit": "quartet-points/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
