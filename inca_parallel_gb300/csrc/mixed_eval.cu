@@ -85,6 +85,13 @@ constexpr int kItemsPerCta = 12;         // persistent passes: work items per re
 #define INCA_FAST_TERMS 1
 #endif
 constexpr float kFastU = 18.0f;
+// One-pass form: each lane works through the noted terms of all its points in one list, two per
+// round (the rounds of a chunk follow the lane with the most terms in all, not the sum over
+// points of the lanes with the most at each point); the per-point correction sums live in
+// shared memory and are added in the same order as point by point, so the bits are the same.
+#ifndef INCA_CORR_COMBINED
+#define INCA_CORR_COMBINED 1
+#endif
 // Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
 // whether inline corrections evaluate two terms per lane and round.
 #ifndef INCA_PASS_CTAS_PER_SM
@@ -277,8 +284,8 @@ __device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int
 // The double-float terms of N records of one class at one point (r_hi + r_lo per dimension);
 // the N evaluations are independent, so N > 1 gives the scheduler independent chains.
 template <int N>
-__device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int L[3], const float (&rh)[3],
-                                          const float (&rl)[3], const float2* __restrict__ tab, f2 (&out)[N]) {
+__device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int L[3], const float (&rh)[N][3],
+                                          const float (&rl)[N][3], const float2* __restrict__ tab, f2 (&out)[N]) {
   const int nc = L[0] + L[1] + L[2] + 3;
   f2 u[N][3];
 #pragma unroll
@@ -286,12 +293,12 @@ __device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int 
     const float s_hi = R[n][0], s_lo = R[n][1];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const float p = __fmul_rn(s_hi, rh[d]);
-      float e = __fmaf_rn(s_hi, rh[d], -p);
+      const float p = __fmul_rn(s_hi, rh[n][d]);
+      float e = __fmaf_rn(s_hi, rh[n][d], -p);
       const f2 t = two_sum(p, R[n][2 + d]);
       e = __fadd_rn(e, t.lo);
-      e = __fmaf_rn(s_hi, rl[d], e);
-      e = __fmaf_rn(s_lo, rh[d], e);
+      e = __fmaf_rn(s_hi, rl[n][d], e);
+      e = __fmaf_rn(s_lo, rh[n][d], e);
       e = __fadd_rn(e, R[n][5 + d]);
       u[n][d] = fast_two_sum(t.hi, e);  // |e| << |t.hi| except near u = 0, where it is harmless
     }
@@ -336,7 +343,7 @@ __device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int 
 __device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry, float rz,
                                    float lx, float ly, float lz, const float2* __restrict__ tab) {
   const int L[3] = {L0, L1, L2};
-  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
+  const float rh[1][3] = {{rx, ry, rz}}, rl[1][3] = {{lx, ly, lz}};
   const float* const Rs[1] = {R};
   f2 out[1];
   term_df_n<1>(Rs, L, rh, rl, tab, out);
@@ -351,7 +358,19 @@ __device__ __noinline__ f2x2 term_df2(const float* __restrict__ Ra, const float*
                                       int L2, float rx, float ry, float rz, float lx, float ly, float lz,
                                       const float2* __restrict__ tab) {
   const int L[3] = {L0, L1, L2};
-  const float rh[3] = {rx, ry, rz}, rl[3] = {lx, ly, lz};
+  const float rh[2][3] = {{rx, ry, rz}, {rx, ry, rz}}, rl[2][3] = {{lx, ly, lz}, {lx, ly, lz}};
+  const float* const Rs[2] = {Ra, Rb};
+  f2 out[2];
+  term_df_n<2>(Rs, L, rh, rl, tab, out);
+  return {out[0], out[1]};
+}
+
+// Two double-float terms (records Ra, Rb of one class) at two points (hi and lo parts of each).
+__device__ __noinline__ f2x2 term_df2p(const float* __restrict__ Ra, const float* __restrict__ Rb, int L0, int L1,
+                                       int L2, float4 ha, float4 la, float4 hb, float4 lb,
+                                       const float2* __restrict__ tab) {
+  const int L[3] = {L0, L1, L2};
+  const float rh[2][3] = {{ha.x, ha.y, ha.z}, {hb.x, hb.y, hb.z}}, rl[2][3] = {{la.x, la.y, la.z}, {lb.x, lb.y, lb.z}};
   const float* const Rs[2] = {Ra, Rb};
   f2 out[2];
   term_df_n<2>(Rs, L, rh, rl, tab, out);
@@ -393,6 +412,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
+  __shared__ float2 corr_s[(kFuse && INCA_CORR_COMBINED) ? kPPT : 1][32];
   const int lane = threadIdx.x;
   if (kFuse)
     for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
@@ -429,6 +449,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         const int j = lane + 32 * p;
         tau[p] = j < T.count ? pt_tau[T.start + j] : HUGE_VALF;
         corr[p] = {0.0f, 0.0f};
+        if (INCA_CORR_COMBINED) corr_s[p][lane] = make_float2(0.0f, 0.0f);
       }
     }
     float box[6];
@@ -488,6 +509,55 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           sa[p] = __fadd_rn(sa[p], e[p]);
         }
       }
+#if INCA_CORR_COMBINED
+      if (kFuse) {
+        // two terms per lane and round, taken in (point, record) order from all the lane's points
+        uint32_t any_left = 0u;
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
+        while (__any_sync(0xffffffffu, any_left != 0u)) {
+          ++nround;
+          int pa = -1, qa = 0, pb = -1, qb = 0;
+#pragma unroll
+          for (int p = 0; p < kPPT; ++p)
+            if (pa < 0 && nm[p]) {
+              pa = p;
+              qa = __ffs(nm[p]) - 1;
+              nm[p] &= nm[p] - 1;
+            }
+#pragma unroll
+          for (int p = 0; p < kPPT; ++p)
+            if (pb < 0 && nm[p]) {
+              pb = p;
+              qb = __ffs(nm[p]) - 1;
+              nm[p] &= nm[p] - 1;
+            }
+          any_left = 0u;
+#pragma unroll
+          for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
+          if (pa >= 0) {
+            const bool two = pb >= 0;
+            if (!two) {  // a lone term is paired with itself and the copy discarded
+              pb = pa;
+              qb = qa;
+            }
+            const int64_t ga = T.start + lane + 32 * pa, gb = T.start + lane + 32 * pb;
+            const f2x2 r = term_df2p(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], phi[ga],
+                                     plo[ga], phi[gb], plo[gb], tab);
+            float2 ca = corr_s[pa][lane];
+            f2 c = df_add(f2{ca.x, ca.y}, r.a);
+            if (two && pb == pa) c = df_add(c, r.b);
+            corr_s[pa][lane] = make_float2(c.hi, c.lo);
+            if (two && pb != pa) {
+              const float2 cb = corr_s[pb][lane];
+              const f2 d = df_add(f2{cb.x, cb.y}, r.b);
+              corr_s[pb][lane] = make_float2(d.hi, d.lo);
+            }
+            ncorr += two ? 2 : 1;
+          }
+        }
+      }
+#else
       if (kFuse) {
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
@@ -519,6 +589,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           }
         }
       }
+#endif
       // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
       const bool fold = ++nfold == kFold;
 #pragma unroll
@@ -530,8 +601,14 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
           sh[p] = sl[p] = 0.0f;
           if (kFuse) {
-            acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-            corr[p] = {0.0f, 0.0f};
+            if (INCA_CORR_COMBINED) {
+              const float2 c = corr_s[p][lane];
+              acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
+              corr_s[p][lane] = make_float2(0.0f, 0.0f);
+            } else {
+              acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+              corr[p] = {0.0f, 0.0f};
+            }
           }
         }
       }
@@ -548,7 +625,14 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
       acc[p] += static_cast<double>(shs[p]) + static_cast<double>(sls[p]);
-      if (kFuse) acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+      if (kFuse) {
+        if (INCA_CORR_COMBINED) {
+          const float2 c = corr_s[p][lane];
+          acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
+        } else {
+          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+        }
+      }
       const int j = lane + 32 * p;
       if (j < T.count) {
         part[pat + T.start + j] = acc[p];
