@@ -225,10 +225,9 @@ struct inca_ctx {
   inca::DevBuf<float2> d_exptab;  // 2^(j/256) table of the double-float exp2
   int64_t prepare_count = 0;      // bumped by every inca_prepare / batch preparation
   cudaGraphExec_t graph_exec = nullptr;
-  int64_t graph_grid = -1, graph_prep = -1, graph_launches = 0;
-  double graph_eps = 0.0;
+  int64_t graph_grid = -1, graph_launches = 0;
+  std::vector<double> graph_sig;  // plan signature of the captured graph (mixed_eval.cu)
   bool graph_fused = false, graph_drop = false;
-  const void* graph_bufs[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 // ---- internal entry points between translation units

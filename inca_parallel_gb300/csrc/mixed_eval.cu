@@ -85,20 +85,9 @@ constexpr int kItemsPerCta = 12;         // persistent passes: work items per re
 #define INCA_FAST_TERMS 1
 #endif
 constexpr float kFastU = 18.0f;
-// One-pass form: each lane works through the noted terms of all its points in one list, two per
-// round (the rounds of a chunk follow the lane with the most terms in all, not the sum over
-// points of the lanes with the most at each point); the per-point correction sums live in
-// shared memory and are added in the same order as point by point, so the bits are the same.
-#ifndef INCA_CORR_COMBINED
-#define INCA_CORR_COMBINED 1
-#endif
-// Resident one-warp CTAs per SM the pass kernels are compiled for (register budget), and
-// whether inline corrections evaluate two terms per lane and round.
+// Resident one-warp CTAs per SM the pass kernels are compiled for (register budget).
 #ifndef INCA_PASS_CTAS_PER_SM
 #define INCA_PASS_CTAS_PER_SM 16
-#endif
-#ifndef INCA_DF_PAIRS
-#define INCA_DF_PAIRS 1
 #endif
 
 // 2^y for y <= 0 in FP32 without systematic bias: y = n + f (n = rint(y), |f| <= 1/2),
@@ -353,18 +342,6 @@ __device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, 
 struct f2x2 {
   f2 a, b;
 };
-// Two double-float terms (records Ra, Rb of one class) at one point.
-__device__ __noinline__ f2x2 term_df2(const float* __restrict__ Ra, const float* __restrict__ Rb, int L0, int L1,
-                                      int L2, float rx, float ry, float rz, float lx, float ly, float lz,
-                                      const float2* __restrict__ tab) {
-  const int L[3] = {L0, L1, L2};
-  const float rh[2][3] = {{rx, ry, rz}, {rx, ry, rz}}, rl[2][3] = {{lx, ly, lz}, {lx, ly, lz}};
-  const float* const Rs[2] = {Ra, Rb};
-  f2 out[2];
-  term_df_n<2>(Rs, L, rh, rl, tab, out);
-  return {out[0], out[1]};
-}
-
 // Two double-float terms (records Ra, Rb of one class) at two points (hi and lo parts of each).
 __device__ __noinline__ f2x2 term_df2p(const float* __restrict__ Ra, const float* __restrict__ Rb, int L0, int L1,
                                        int L2, float4 ha, float4 la, float4 hb, float4 lb,
@@ -412,7 +389,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
-  __shared__ float2 corr_s[(kFuse && INCA_CORR_COMBINED) ? kPPT : 1][32];
+  // per-point double-float correction sums of the one-pass form (shared memory: the rounds of
+  // inline corrections reach any of the lane's points)
+  __shared__ float2 corr_s[kFuse ? kPPT : 1][32];
   const int lane = threadIdx.x;
   if (kFuse)
     for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
@@ -442,14 +421,12 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     float rh[3][kPPT], rl[3][kPPT];
     load_points(phi, plo, T, lane, rh, rl);
     float tau[kPPT];
-    f2 corr[kPPT];
     if (kFuse) {
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         const int j = lane + 32 * p;
         tau[p] = j < T.count ? pt_tau[T.start + j] : HUGE_VALF;
-        corr[p] = {0.0f, 0.0f};
-        if (INCA_CORR_COMBINED) corr_s[p][lane] = make_float2(0.0f, 0.0f);
+        corr_s[p][lane] = make_float2(0.0f, 0.0f);
       }
     }
     float box[6];
@@ -509,7 +486,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           sa[p] = __fadd_rn(sa[p], e[p]);
         }
       }
-#if INCA_CORR_COMBINED
       if (kFuse) {
         // two terms per lane and round, taken in (point, record) order from all the lane's points
         uint32_t any_left = 0u;
@@ -557,39 +533,6 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           }
         }
       }
-#else
-      if (kFuse) {
-#pragma unroll
-        for (int p = 0; p < kPPT; ++p) {
-          // two terms per lane and round (independent chains); a lone last term is paired
-          // with itself and the copy discarded, so the lanes of a round run the same code
-          uint32_t mm = nm[p];
-          while (__any_sync(0xffffffffu, mm != 0u)) {
-            ++nround;
-            if (!INCA_DF_PAIRS && mm) {
-              const int q = __ffs(mm) - 1;
-              mm &= mm - 1;
-              const f2 tdf = term_df(st + q * sg.stride32, L[0], L[1], L[2], rh[0][p], rh[1][p],
-                                     rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
-              corr[p] = df_add(corr[p], tdf);
-              ++ncorr;
-            } else if (mm) {
-              const int qa = __ffs(mm) - 1;
-              mm &= mm - 1;
-              const bool two = mm != 0u;
-              const int qb = two ? __ffs(mm) - 1 : qa;
-              if (two) mm &= mm - 1;
-              const f2x2 r = term_df2(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2],
-                                      rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p],
-                                      rl[2][p], tab);
-              corr[p] = df_add(corr[p], r.a);
-              if (two) corr[p] = df_add(corr[p], r.b);
-              ncorr += two ? 2 : 1;
-            }
-          }
-        }
-      }
-#endif
       // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
       const bool fold = ++nfold == kFold;
 #pragma unroll
@@ -601,14 +544,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           acc[p] += static_cast<double>(sh[p]) + static_cast<double>(sl[p]);
           sh[p] = sl[p] = 0.0f;
           if (kFuse) {
-            if (INCA_CORR_COMBINED) {
-              const float2 c = corr_s[p][lane];
-              acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
-              corr_s[p][lane] = make_float2(0.0f, 0.0f);
-            } else {
-              acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-              corr[p] = {0.0f, 0.0f};
-            }
+            const float2 c = corr_s[p][lane];
+            acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
+            corr_s[p][lane] = make_float2(0.0f, 0.0f);
           }
         }
       }
@@ -626,12 +564,8 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     for (int p = 0; p < kPPT; ++p) {
       acc[p] += static_cast<double>(shs[p]) + static_cast<double>(sls[p]);
       if (kFuse) {
-        if (INCA_CORR_COMBINED) {
-          const float2 c = corr_s[p][lane];
-          acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
-        } else {
-          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-        }
+        const float2 c = corr_s[p][lane];
+        acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
       }
       const int j = lane + 32 * p;
       if (j < T.count) {
@@ -1721,18 +1655,41 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   return INCA_OK;
 }
 
+// Everything a captured launch sequence holds by value: the plan's sizes, knobs and buffer
+// addresses, and the addresses of the records, chunks, classes and sorted grid it reads. Two
+// evaluations with the same signature run the same graph (the data in those buffers is read when
+// the graph runs), so a graph stays valid across inca_prepare calls that give tables of the same
+// shape, and a new schedule, tolerance or knob forces a new capture.
+static std::vector<double> plan_signature(const inca_ctx* c, const MixedPlan& P) {
+  auto a = [](const void* p) { return static_cast<double>(reinterpret_cast<uintptr_t>(p)); };
+  std::vector<double> s = {double(P.fused), double(P.mode), double(P.nseg), double(P.emode), double(P.nmol),
+                           a(P.seg_of), double(P.ngrid), double(P.nwt), double(P.ngroups), double(P.nitems),
+                           double(P.npart), double(P.ndrop), double(P.ns), double(P.nitems_s), double(P.npart_s),
+                           double(P.nctas), double(P.nctas_s), double(P.gblk), double(P.tblk),
+                           double(P.stage_floats), double(P.dsmem), P.eps, P.tau_scale, P.safety, P.drop_frac,
+                           P.nq, a(P.p1), a(P.q1), a(P.mwdev), a(P.mws), a(P.tab), a(c->d_scratch.p),
+                           a(c->d_scratch_s.p), a(c->d_ivec.p), a(c->d_chunks.p), a(c->d_classes.p),
+                           a(c->d_rec32.p), a(c->d_phi.p), a(c->d_plo.p), a(c->d_tiles.p), a(c->d_wtbox.p),
+                           a(c->d_perm.p), a(c->d_phi_s.p), a(c->d_plo_s.p), a(c->d_tiles_s.p),
+                           a(c->d_wtbox_s.p), a(c->d_perm_s.p), a(c->d_w.p)};
+  return s;
+}
+
 int eval_mixed_graph(inca_ctx* c, double eps) {
   if (cube_separable(c)) return eval_cube_separable(c, eps);  // a few launches: run directly
   if (c->chunks.empty()) return eval_mixed(c, eps);
-  const void* bufs[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};
-  const bool fresh = c->graph_exec && c->graph_grid == c->grid_version && c->graph_prep == c->prepare_count &&
-                     c->graph_eps == eps && std::equal(bufs, bufs + 4, c->graph_bufs);
+  bool fresh = false;
+  MixedPlan P;
+  int st = 0;
+  if (c->graph_exec && c->graph_grid == c->grid_version) {
+    if ((st = mixed_plan(c, eps, P))) return st;
+    fresh = plan_signature(c, P) == c->graph_sig;
+  }
   if (!fresh) {
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
-    int st = eval_mixed(c, eps);  // sizes every buffer and fills every cache first
+    st = eval_mixed(c, eps);  // sizes every buffer and fills every cache first
     if (st) return st;
-    MixedPlan P;
     if ((st = mixed_plan(c, eps, P))) return st;
     cudaGraph_t g = nullptr;
     INCA_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1749,17 +1706,12 @@ int eval_mixed_graph(inca_ctx* c, double eps) {
     cudaGraphDestroy(g);
     if (e) return cuda_error(c, e, "graph instantiate");
     c->graph_grid = c->grid_version;
-    c->graph_prep = c->prepare_count;
-    c->graph_eps = eps;
+    c->graph_sig = plan_signature(c, P);
     c->graph_fused = P.fused;
     c->graph_drop = P.fused && P.drop_frac > 0.0;
-    const void* now[4] = {c->d_scratch.p, c->d_scratch_s.p, c->d_ivec.p, c->d_exptab.p};
-    std::copy(now, now + 4, c->graph_bufs);
     return INCA_OK;  // this call's result came from the eager run
   }
-  MixedPlan P;
-  int st = mixed_plan(c, eps, P);  // same sizes: carves the same buffers, uploads the same tables
-  if (st) return st;
+  // the plan of this call (same signature) has uploaded its tables; the graph runs the passes
   INCA_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
   c->launches += c->graph_launches;
   bool retry = false;

@@ -155,8 +155,9 @@ int inca_autotune(inca_ctx* ctx, double tol, int32_t reps, inca_tuning* chosen);
 int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);
 
 /* inca_eval replayed from a CUDA graph (INCA_MIXED; INCA_FP64 runs as inca_eval). The first
- * call after the grid, the records (inca_prepare, inca_batch_prepare) or tol change evaluates
- * normally and captures the evaluation's launch sequence; later calls launch the captured graph,
+ * call after the grid, tol, the schedule (inca_set_tuning, inca_autotune) or the shape of the
+ * record tables changes evaluates normally and captures the evaluation's launch sequence; later
+ * calls launch the captured graph,
  * which runs every pass without returning to the host in between. Cube lattices evaluated by
  * the separable form (two launches, nothing to plan) run as inca_eval. No counterpart in the
  * reference. */

@@ -132,3 +132,29 @@ def test_autotune_keeps_tolerance(ctx, scan_fp64):
             assert rel.max() <= 1e-8, (ipc, stride, safety, rel.max())
     finally:
         ctx.set_tuning()
+
+
+def test_graph_follows_schedule_knobs_and_reprepare(ctx, monkeypatch):
+    # a captured graph holds the plan's sizes by value: a new schedule or knob must be captured
+    # anew (results equal to the eager run with that schedule), and a new inca_prepare of the
+    # same input gives tables of the same shape, which the graph keeps serving
+    ctx.grid_scan(*SCAN)
+    ref = ctx.eval(mode=1, tol=1e-8)
+    ctx.eval_graph(mode=1, tol=1e-8)
+    np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), ref)
+    try:
+        ctx.set_tuning(4, 32, 0.7, 0.1)
+        eager = ctx.eval(mode=1, tol=1e-8)
+        for _ in range(2):
+            np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+    finally:
+        ctx.set_tuning()
+    monkeypatch.setenv("INCA_DROP_FRACTION", "0")
+    eager = ctx.eval(mode=1, tol=1e-8)
+    for _ in range(2):
+        np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+    monkeypatch.delenv("INCA_DROP_FRACTION")
+    np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), ref)
+    ctx.prepare(THRESH)
+    for _ in range(2):
+        np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), ref)
