@@ -1623,7 +1623,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   if (st) return st;
   *default_ms = best;
   const int ipcs[] = {4, 8, 12, 24, 48};
-  const int strides[] = {8, 16, 32};
+  const int strides[] = {8, 16, 32, 64};
   const double safeties[] = {0.3, 0.5, 0.7};
   const double drops[] = {0.02, 0.05, 0.1, 0.2};
   auto consider = [&](Sched s) -> int {
