@@ -451,12 +451,17 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
       const float* st = S.buf(k);
-      const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
+      // the class's degrees and record stride pass through a warp reduction: its result is
+      // warp-uniform by construction, so the degree tests and Horner loops of every term are
+      // uniform branches (no reconvergence bookkeeping) and their counters leave the vector pipes
+      const int L[3] = {__reduce_max_sync(0xffffffffu, sg.L[0]), __reduce_max_sync(0xffffffffu, sg.L[1]),
+                        __reduce_max_sync(0xffffffffu, sg.L[2])};
+      const int rs = __reduce_max_sync(0xffffffffu, sg.stride32);
       float umax = HUGE_VALF;
-      const float lb = lane < w.count ? log2_bound(st + lane * sg.stride32, L, box, nullptr, &umax) : -HUGE_VALF;
+      const float lb = lane < w.count ? log2_bound(st + lane * rs, L, box, nullptr, &umax) : -HUGE_VALF;
       uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
       const uint32_t fast = INCA_FAST_TERMS ? __ballot_sync(0xffffffffu, lane < w.count && umax < kFastU &&
-                                                                           st[lane * sg.stride32 + 11] <= 100.0f)
+                                                                           st[lane * rs + 11] <= 100.0f)
                                             : 0u;
       if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
       if (lane == 0) {
@@ -471,9 +476,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         m &= m - 1;
         float t[kPPT], e[kPPT];
         if ((fast >> q) & 1u)
-          terms32<kPPT, true, false>(st + q * sg.stride32, L, rh, rl, t, e);
+          terms32<kPPT, true, false>(st + q * rs, L, rh, rl, t, e);
         else
-          terms32<kPPT, true, true>(st + q * sg.stride32, L, rh, rl, t, e);
+          terms32<kPPT, true, true>(st + q * rs, L, rh, rl, t, e);
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
           if (kFuse && e[p] > tau[p]) {
@@ -518,7 +523,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
               qb = qa;
             }
             const int64_t ga = T.start + lane + 32 * pa, gb = T.start + lane + 32 * pb;
-            const f2x2 r = term_df2p(st + qa * sg.stride32, st + qb * sg.stride32, L[0], L[1], L[2], phi[ga],
+            const f2x2 r = term_df2p(st + qa * rs, st + qb * rs, L[0], L[1], L[2], phi[ga],
                                      plo[ga], phi[gb], plo[gb], tab);
             float2 ca = corr_s[pa][lane];
             f2 c = df_add(f2{ca.x, ca.y}, r.a);
