@@ -161,7 +161,10 @@ __device__ __forceinline__ void poly2_pts(int L, const float* __restrict__ C, co
 // Explicit round-to-nearest intrinsics only, so both passes produce the same bits.
 // kSafe = false (records whose |u_d| stays below kFastU over the tile, and ks <= 100): the
 // clamps of u and y are left out; they would change nothing there, so the bits are the same.
-template <int NP, bool kErr, bool kSafe = true>
+// kComp = false (threshold estimates only): u_d = fma(s_hi, r_hi, b_hi) without the low parts,
+// an absolute error of about u32 (|s r| + |b|) instead of u32 |u_d|; the error bound keeps its
+// form, so it estimates the bound of the compensated term at that point.
+template <int NP, bool kErr, bool kSafe = true, bool kComp = true>
 __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L[3], const float (&rh)[3][NP],
                                         const float (&rl)[3][NP], float (&t)[NP], float (&err)[NP]) {
   // the record head in three 16-byte loads (records are 16-byte aligned: strides of 4 floats)
@@ -177,9 +180,13 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
     const float b_hi = bh[d], b_lo = bl[d];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
-      float t1 = __fmaf_rn(s_lo, rh[d][p], b_lo);
-      t1 = __fmaf_rn(s_hi, rl[d][p], t1);
-      u[d][p] = __fadd_rn(__fmaf_rn(s_hi, rh[d][p], b_hi), t1);
+      if (kComp) {
+        float t1 = __fmaf_rn(s_lo, rh[d][p], b_lo);
+        t1 = __fmaf_rn(s_hi, rl[d][p], t1);
+        u[d][p] = __fadd_rn(__fmaf_rn(s_hi, rh[d][p], b_hi), t1);
+      } else {
+        u[d][p] = __fmaf_rn(s_hi, rh[d][p], b_hi);
+      }
     }
   }
   float E[NP], Y[NP];
@@ -377,7 +384,11 @@ __device__ __forceinline__ void load_points(const float4* __restrict__ phi, cons
 //   lanes note (quartet, point) in a mask, and after each chunk the warp evaluates the noted
 //   terms in double-float, each lane working down its own list (the chunk is class-uniform,
 //   so the lanes run the same instruction sequence on different quartets).
-template <bool kFuse>
+// kEst = true (with kFuse = false): the estimate pass of the one-pass form on the grid sample.
+//   Its sums only set the estimated thresholds (an estimate that is off costs corrections or a
+//   band pass, never accuracy), so its terms skip the compensation of u (kComp = false) and are
+//   summed in plain FP32, moved to FP64 after every chunk; the error bounds are the same.
+template <bool kFuse, bool kEst = false>
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
@@ -386,6 +397,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop, double* __restrict__ part,
         double* __restrict__ part_abs, double* __restrict__ drop_mass, unsigned long long* __restrict__ work,
         unsigned long long* __restrict__ stats, int* __restrict__ err) {
+  static_assert(!(kFuse && kEst), "the estimate pass has no corrections");
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
@@ -476,18 +488,22 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         m &= m - 1;
         float t[kPPT], e[kPPT];
         if ((fast >> q) & 1u)
-          terms32<kPPT, true, false>(st + q * rs, L, rh, rl, t, e);
+          terms32<kPPT, true, false, !kEst>(st + q * rs, L, rh, rl, t, e);
         else
-          terms32<kPPT, true, true>(st + q * rs, L, rh, rl, t, e);
+          terms32<kPPT, true, true, !kEst>(st + q * rs, L, rh, rl, t, e);
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
           if (kFuse && e[p] > tau[p]) {
             nm[p] |= 1u << q;
             t[p] = 0.0f;
           }
-          const f2 s2 = two_sum(sh[p], t[p]);
-          sh[p] = s2.hi;
-          sl[p] = __fadd_rn(sl[p], s2.lo);
+          if (kEst) {
+            sh[p] = __fadd_rn(sh[p], t[p]);
+          } else {
+            const f2 s2 = two_sum(sh[p], t[p]);
+            sh[p] = s2.hi;
+            sl[p] = __fadd_rn(sl[p], s2.lo);
+          }
           sa[p] = __fadd_rn(sa[p], e[p]);
         }
       }
@@ -538,8 +554,9 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
           }
         }
       }
-      // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks
-      const bool fold = ++nfold == kFold;
+      // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks (the plain
+      // sums of the estimate pass after every chunk)
+      const bool fold = ++nfold == (kEst ? 1 : kFold);
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         const f2 r = fast_two_sum(sh[p], sl[p]);
@@ -1427,7 +1444,8 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   // ---- estimates from the grid sample (one-pass form): thresholds and drop thresholds
   if (P.fused) {
     const int64_t ns = P.ns;
-    INCA_LAUNCH(c, k_pass1<false>, P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p, c->d_rec32.p,
+    INCA_LAUNCH(c, (k_pass1<false, true>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p,
+                c->d_rec32.p,
                 c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, P.nitems_s, P.stage_floats, nullptr,
                 nullptr, nullptr, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw);
     INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
