@@ -1333,7 +1333,11 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   if (P.fused) {
     P.ns = c->nsample;
     int64_t ndrop_s = 0;
-    hmw_s = work_table(c->mol_span_s, c->mol_chunks, c->num_sms, ipc, &P.nitems_s, &P.npart_s, &ndrop_s);
+    // the sample has 1/stride of the tiles: with the main pass's item count its items would
+    // hold a chunk or two each and their fixed costs (points, box, first stage, partial sums)
+    // would rival the work; at most 4 items per CTA measured best
+    const int ipc_s = static_cast<int>(env_knob("INCA_SAMPLE_ITEMS_PER_CTA", std::min(ipc, 4), 1, 1e6));
+    hmw_s = work_table(c->mol_span_s, c->mol_chunks, c->num_sms, ipc_s, &P.nitems_s, &P.npart_s, &ndrop_s);
     P.nctas_s = persistent_ctas(P.nitems_s, c->num_sms);
   }
   // survivors of the largest molecule: an upper bound on the terms left out at a point
