@@ -4,7 +4,8 @@ The FP64 GPU form is checked against the oracle at 1e-12 in test_gpu_parity.py a
 the full-size oracle here. Tolerances: 1e-8 relative on each I(s), 1e-10 relative on the radial
 integral, 1e-8 of max|I| on the vector cube. The threshold estimates are also forced to both
 extremes (INCA_EST_SAFETY): 0 corrects every term in the one pass; 1e6 leaves the corrections
-to the correction pass, which must then run and still meet the tolerance.
+to the correction pass, which must then run and still meet the tolerance. The estimate pass's
+work split (INCA_SAMPLE_ITEMS_PER_CTA) is driven to 1, 4 and 48 items per CTA.
 """
 import numpy as np
 import pytest
@@ -60,6 +61,20 @@ def test_estimate_extremes(ctx, scan_fp64, monkeypatch, safety):
     if safety == "1e6":
         assert ctx.phases()["pass2_ms"] > 0.0
         assert ctx.stats()["precise_pairs"] > 0
+
+
+@pytest.mark.parametrize("items", ["1", "4", "48"])
+def test_estimate_pass_items(ctx, scan_fp64, monkeypatch, items):
+    # the estimate pass's work split (INCA_SAMPLE_ITEMS_PER_CTA) changes its partial sums, hence
+    # the estimated thresholds and the set of inline corrections, never the tolerance met; a
+    # captured graph follows the knob
+    monkeypatch.setenv("INCA_SAMPLE_ITEMS_PER_CTA", items)
+    I = _scan_mixed(ctx)
+    rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+    assert rel.max() <= 1e-8, rel.max()
+    eager = ctx.eval(mode=1, tol=1e-8)
+    np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+    np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
 
 
 def test_one_pass_deterministic(ctx):
