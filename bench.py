@@ -278,7 +278,8 @@ def gpu_arm(args):
     cube_err = float(np.abs(cube["mixed"]["I"] - cube["fp64"]["I"]).max() / np.abs(cube["fp64"]["I"]).max())
     cube_qp = counts[2] * int(np.prod(CUBE[2]))
 
-    # end to end through the C ABI with host buffers (the driver's call sequence), tuned schedule;
+    # end to end through the C ABI with host buffers (the call sequence of the Fortran program's
+    # bind(C) shim), tuned schedule;
     # the quartet input and the I(r) output live in pinned host memory
     ctx.set_tuning(sched["items_per_cta"], sched["sample_stride"], sched["estimate_safety"], sched["drop_fraction"])
     ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
