@@ -1,5 +1,7 @@
 """Unit checks of the oracle's building blocks against independent implementations (CPU)."""
 import math
+import os
+import re
 
 import numpy as np
 import pytest
@@ -29,6 +31,36 @@ def test_lebedev_rules_match_scipy(nang, order):
     np.testing.assert_allclose(mine, theirs, atol=2e-12)
 
 
+def _sphere_moment(a, b, c):
+    """Mean of x^a y^b z^c over the unit sphere: 2 G((a+1)/2) G((b+1)/2) G((c+1)/2) /
+    G((a+b+c+3)/2) / (4 pi) when a, b, c are all even, else 0."""
+    if a % 2 or b % 2 or c % 2:
+        return 0.0
+    g = math.lgamma((a + 1) / 2) + math.lgamma((b + 1) / 2) + math.lgamma((c + 1) / 2)
+    return 2.0 * math.exp(g - math.lgamma((a + b + c + 3) / 2)) / (4.0 * math.pi)
+
+
+@pytest.mark.parametrize("nang,order", list(zip(RULES, ORDERS)))
+def test_lebedev_rules_exact(nang, order):
+    # independent of any library: a rule of algebraic order p averages every monomial of degree
+    # <= p over the sphere exactly (checked up to degree 24, where the moments stay well scaled)
+    x, y, z, w = O.lebedev(nang)
+    assert len(w) == nang
+    deg = min(order, 24)
+    for a in range(deg + 1):
+        xa = x ** a
+        for b in range(deg + 1 - a):
+            xyab = xa * y ** b
+            for c in range(deg + 1 - a - b):
+                got = float(np.dot(w, xyab * z ** c))
+                assert abs(got - _sphere_moment(a, b, c)) < 1e-13, (nang, a, b, c, got)
+    # and one degree beyond the order is not integrated exactly by the smallest rules
+    if order <= 7:
+        errs = [abs(float(np.dot(w, x ** a * y ** b * z ** (order + 1 - a - b))) - _sphere_moment(a, b, order + 1 - a - b))
+                for a in range(order + 2) for b in range(order + 2 - a)]
+        assert max(errs) > 1e-6
+
+
 @pytest.mark.parametrize("n", [1, 2, 5, 50, 75, 150])
 def test_gauss_legendre(n):
     t, w = O.gauleg(n)
@@ -38,19 +70,30 @@ def test_gauss_legendre(n):
     np.testing.assert_allclose(w, wn, rtol=1e-10, atol=1e-15)
 
 
+def _c_table(src, name):
+    """The rows of `static const double name[R][C] = {{...}, ...};` in a generated header."""
+    body = src[src.index(name + "["):]
+    body = body[body.index("{") + 1:body.index("};")]
+    return [[float(x) for x in row.split(",") if x.strip()] for row in re.findall(r"\{([^{}]*)\}", body)]
+
+
 def test_hermite_table():
-    import ctypes  # noqa: F401
-    # nodes/weights of the generated table integrate x^(2k) exp(-x^2) exactly
-    import re
-    import os
+    # the generated table's n-node rule integrates x^(2k) exp(-x^2) exactly for 2k < 2n
+    # (moments Gamma(k + 1/2)), its nodes are symmetric and ascending, and it agrees with
+    # numpy's Gauss-Hermite rule
     src = open(os.path.join(O.ROOT, "inca_parallel_gb300", "csrc", "hermite_table.h")).read()
+    nodes, weights = _c_table(src, "kNode"), _c_table(src, "kWeight")
+    assert len(nodes) == len(weights) == 12
     for n in range(1, 12):
-        xn, wn = np.polynomial.hermite.hermgauss(n)
-        # compare by moments: sum w x^(2k) = Gamma(k+1/2)
+        x, w = np.array(nodes[n][:n]), np.array(weights[n][:n])
+        assert np.all(np.diff(x) > 0) and np.allclose(x, -x[::-1], rtol=0, atol=1e-15)
+        assert np.all(w > 0) and np.all(np.array(weights[n][n:]) == 0.0)
         for k in range(n):
             mom = math.gamma(k + 0.5)
-            assert abs((wn * xn ** (2 * k)).sum() - mom) < 1e-12 * max(1, mom)
-    assert "kNode" in src and "kWeight" in src
+            assert abs((w * x ** (2 * k)).sum() - mom) < 1e-12 * max(1.0, mom), (n, k)
+        xn, wn = np.polynomial.hermite.hermgauss(n)
+        np.testing.assert_allclose(x, xn, rtol=1e-13, atol=1e-14)
+        np.testing.assert_allclose(w, wn, rtol=1e-12)
 
 
 @pytest.mark.parametrize("seed", range(5))
