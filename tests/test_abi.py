@@ -1,5 +1,4 @@
 """The C-ABI library builds, loads and exports every entry point of include/inca_gpu.h (CPU)."""
-import ctypes
 import os
 import re
 

@@ -6,7 +6,6 @@ is held to much tighter bounds here: the goldens carry ~16 digits except the .ra
 9 digits).
 """
 import numpy as np
-import pytest
 
 import oracle_lib as O
 
