@@ -88,6 +88,18 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_ja8.release();
   c->d_s1.release();
   c->d_s2.release();
+  c->d_pkey.release();
+  c->d_pkey2.release();
+  c->d_pukeys.release();
+  c->d_pidx.release();
+  c->d_pidx2.release();
+  c->d_pucounts.release();
+  c->d_ptmp.release();
+  c->d_pbad.release();
+  c->d_pnruns.release();
+  c->d_pn1.release();
+  c->d_roff.release();
+  c->d_rsum.release();
   c->d_classes.release();
   c->d_chunks.release();
   c->d_rec64.release();

@@ -502,22 +502,20 @@ int radial_integral_device(inca_ctx* c, double* total, double* vee, double* per_
   std::vector<int64_t> off(c->nquad + 1, 0);
   for (int64_t i = 0; i < c->ngrid; ++i) off[tags[i] + 1]++;
   for (int q = 0; q < c->nquad; ++q) off[q + 1] += off[q];
-  DevBuf<int64_t> doff;
-  DevBuf<double> o1, o2;
-  if (doff.reserve(c->nquad + 1) || o1.reserve(c->nquad) || o2.reserve(c->nquad)) {
-    doff.release(); o1.release(); o2.release();
+  if (c->d_roff.reserve(c->nquad + 1) || c->d_rsum.reserve(2 * static_cast<size_t>(c->nquad)))
     return set_error(c, INCA_E_NOMEM, "radial integral");
-  }
-  cudaError_t e = cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (c->nquad + 1), cudaMemcpyHostToDevice, c->stream);
+  int64_t* doff = c->d_roff.p;
+  double* o1 = c->d_rsum.p;
+  double* o2 = c->d_rsum.p + c->nquad;
+  cudaError_t e = cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (c->nquad + 1), cudaMemcpyHostToDevice, c->stream);
   if (!e) {
-    INCA_LAUNCH(c, k_seg_dot, c->nquad, 256, 0, c->nquad, doff.p, c->d_ivec.p, c->d_w.p, c->d_wvee.p, o1.p, o2.p);
+    INCA_LAUNCH(c, k_seg_dot, c->nquad, 256, 0, c->nquad, doff, c->d_ivec.p, c->d_w.p, c->d_wvee.p, o1, o2);
     e = cudaGetLastError();
   }
   std::vector<double> h1(c->nquad), h2(c->nquad);
-  if (!e) e = cudaMemcpyAsync(h1.data(), o1.p, sizeof(double) * c->nquad, cudaMemcpyDeviceToHost, c->stream);
-  if (!e) e = cudaMemcpyAsync(h2.data(), o2.p, sizeof(double) * c->nquad, cudaMemcpyDeviceToHost, c->stream);
+  if (!e) e = cudaMemcpyAsync(h1.data(), o1, sizeof(double) * c->nquad, cudaMemcpyDeviceToHost, c->stream);
+  if (!e) e = cudaMemcpyAsync(h2.data(), o2, sizeof(double) * c->nquad, cudaMemcpyDeviceToHost, c->stream);
   if (!e) e = cudaStreamSynchronize(c->stream);
-  doff.release(); o1.release(); o2.release();
   if (e) return cuda_error(c, e, "radial integral");
   double t = 0, v = 0;
   for (int q = 0; q < c->nquad; ++q) {
@@ -537,20 +535,14 @@ int radial_plot_device(inca_ctx* c, double* rintra) {
   const int ns = c->nradi;
   std::vector<int64_t> off(ns + 1, 0);
   for (int s = 0; s < ns; ++s) off[s + 1] = off[s] + c->h_smn[s];
-  DevBuf<int64_t> doff;
-  DevBuf<double> o1;
-  if (doff.reserve(ns + 1) || o1.reserve(ns)) {
-    doff.release(); o1.release();
-    return set_error(c, INCA_E_NOMEM, "radial plot");
-  }
-  cudaError_t e = cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, c->stream);
+  if (c->d_roff.reserve(ns + 1) || c->d_rsum.reserve(ns)) return set_error(c, INCA_E_NOMEM, "radial plot");
+  cudaError_t e = cudaMemcpyAsync(c->d_roff.p, off.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, c->stream);
   if (!e) {
-    INCA_LAUNCH(c, k_seg_dot, ns, 256, 0, ns, doff.p, c->d_ivec.p, c->d_w.p, nullptr, o1.p, nullptr);
+    INCA_LAUNCH(c, k_seg_dot, ns, 256, 0, ns, c->d_roff.p, c->d_ivec.p, c->d_w.p, nullptr, c->d_rsum.p, nullptr);
     e = cudaGetLastError();
   }
-  if (!e) e = cudaMemcpyAsync(rintra, o1.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream);
+  if (!e) e = cudaMemcpyAsync(rintra, c->d_rsum.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream);
   if (!e) e = cudaStreamSynchronize(c->stream);
-  doff.release(); o1.release();
   if (e) return cuda_error(c, e, "radial plot");
   return INCA_OK;
 }

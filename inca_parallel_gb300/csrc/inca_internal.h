@@ -144,6 +144,13 @@ struct inca_ctx {
   inca::DevBuf<double> d_ja8;  // JA8 of every primitive pair (screening)
   inca::DevBuf<double> d_s1, d_s2;
   bool have_screen_values = false;
+  // scratch of inca_prepare (sort keys and indices, radix-sort temporary storage, run-length
+  // encoding of the classes, counters); kept between calls for lists of moderate size
+  inca::DevBuf<uint32_t> d_pkey, d_pkey2, d_pukeys;
+  inca::DevBuf<int64_t> d_pidx, d_pidx2, d_pucounts;
+  inca::DevBuf<unsigned char> d_ptmp;
+  inca::DevBuf<int> d_pbad, d_pnruns;
+  inca::DevBuf<unsigned long long> d_pn1;
 
   // survivors, grouped by class
   int64_t nsurv = 0;
@@ -176,6 +183,9 @@ struct inca_ctx {
   inca::DevBuf<double> d_px, d_py, d_pz, d_w, d_wvee;
   inca::DevBuf<int> d_cmap;
   inca::DevBuf<double> d_ivec;
+  // scratch of the per-shell / per-centre reductions (segment offsets, sums), kept between calls
+  inca::DevBuf<int64_t> d_roff;
+  inca::DevBuf<double> d_rsum;
   bool evaluated = false;
   int64_t grid_version = 0;  // bumped by every grid builder
 

@@ -189,6 +189,9 @@ __global__ void k_pair_ja8(int nprim, const PrimD* __restrict__ prims, double* _
 }
 
 constexpr int kPairTableMax = 4096;
+// inca_prepare keeps its sort scratch (about 24 B per quartet plus the radix sort's temporary
+// storage) in the context for lists of up to 2^26 quartets (about 1.6 GB)
+constexpr int64_t kPrepKeepQuartets = int64_t(1) << 26;
 
 // One quartet (src/mod_intracule.f90:282-343). Returns 0 / 1 (screen 1) / 3 (both).
 // Jtab (optional): the JA8 table of k_pair_ja8.
@@ -437,16 +440,31 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
       return set_error(c, INCA_E_NOMEM, "screening values");
   }
   c->have_screen_values = keep_values;
-  // sort buffers
-  DevBuf<uint32_t> key, key2;
-  DevBuf<int64_t> idx, idx2;
-  DevBuf<int> bad;
-  DevBuf<unsigned long long> n1dev;
-  if (key.reserve(n) || key2.reserve(n) || idx.reserve(n) || idx2.reserve(n) || bad.reserve(1) || n1dev.reserve(1)) {
+  // sort and run-length scratch, owned by the context: kept between calls for lists of up to
+  // kPrepKeepQuartets quartets (a repeated preparation then allocates and frees nothing, and no
+  // cudaFree stalls the stream), given back after the call for larger lists
+  DevBuf<uint32_t>& key = c->d_pkey;
+  DevBuf<uint32_t>& key2 = c->d_pkey2;
+  DevBuf<int64_t>& idx = c->d_pidx;
+  DevBuf<int64_t>& idx2 = c->d_pidx2;
+  DevBuf<int>& bad = c->d_pbad;
+  DevBuf<unsigned long long>& n1dev = c->d_pn1;
+  DevBuf<unsigned char>& tmp = c->d_ptmp;
+  DevBuf<uint32_t>& ukeys = c->d_pukeys;
+  DevBuf<int64_t>& ucounts = c->d_pucounts;
+  DevBuf<int>& nruns = c->d_pnruns;
+  auto release_all = [&]() {
     key.release(); key2.release(); idx.release(); idx2.release(); bad.release(); n1dev.release();
+    tmp.release(); ukeys.release(); ucounts.release(); nruns.release();
+  };
+  const bool keep_scratch = n <= kPrepKeepQuartets;
+  auto cleanup = [&]() {
+    if (!keep_scratch) release_all();
+  };
+  if (key.reserve(n) || key2.reserve(n) || idx.reserve(n) || idx2.reserve(n) || bad.reserve(1) || n1dev.reserve(1)) {
+    release_all();
     return set_error(c, INCA_E_NOMEM, "inca_prepare: sort buffers");
   }
-  auto cleanup = [&]() { key.release(); key2.release(); idx.release(); idx2.release(); bad.release(); n1dev.release(); };
   cudaError_t e = cudaMemsetAsync(bad.p, 0, sizeof(int), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(n1dev.p, 0, sizeof(unsigned long long), c->stream);
   const int bs = 128;
@@ -473,15 +491,11 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   size_t tmp_bytes = 0;
   if (e == cudaSuccess)
     e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 32, c->stream);
-  DevBuf<unsigned char> tmp;
-  if (e == cudaSuccess) e = tmp.reserve(tmp_bytes);
+  if (e == cudaSuccess && tmp_bytes > tmp.n) e = tmp.reserve(tmp_bytes);
   if (e == cudaSuccess)
     e = cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, key.p, key2.p, idx.p, idx2.p, n, 0, 32, c->stream);
   // class histogram from the sorted keys: copy keys to host (4 B per quartet) is too
   // large for big lists, so run-length encode on the device.
-  DevBuf<uint32_t> ukeys;
-  DevBuf<int64_t> ucounts;
-  DevBuf<int> nruns;
   if (e == cudaSuccess) e = ukeys.reserve(4096);
   if (e == cudaSuccess) e = ucounts.reserve(4096);
   if (e == cudaSuccess) e = nruns.reserve(1);
@@ -503,15 +517,12 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     e = cudaMemcpy(hk.data(), ukeys.p, sizeof(uint32_t) * h_runs, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(hcnt.data(), ucounts.p, sizeof(int64_t) * h_runs, cudaMemcpyDeviceToHost);
   }
-  ukeys.release(); ucounts.release(); nruns.release();
   if (e != cudaSuccess) {
-    cleanup();
-    tmp.release();
+    release_all();
     return cuda_error(c, e, "inca_prepare (screening)");
   }
   if (h_bad) {
     cleanup();
-    tmp.release();
     return set_error(c, INCA_E_ARG, "inca_prepare: quartet index outside 1..nprim");
   }
   // class segments
@@ -550,7 +561,6 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     const int mol = c->classes[s].mol;
     if (mol < 0 || mol >= nmol) {
       cleanup();
-      tmp.release();
       return set_error(c, INCA_E_STATE, "inca_prepare: molecule index outside the batch");
     }
     if (!seen[mol]) {
@@ -574,8 +584,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
       c->d_surv_src.reserve(std::max<int64_t>(nsurv, 1)) ||
       c->d_classes.reserve(std::max<size_t>(c->classes.size(), 1)) ||
       c->d_chunks.reserve(std::max<size_t>(c->chunks.size(), 1))) {
-    cleanup();
-    tmp.release();
+    release_all();
     return set_error(c, INCA_E_NOMEM, "inca_prepare: survivor records");
   }
   if (!c->classes.empty())
@@ -591,9 +600,11 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    release_all();
+    return cuda_error(c, e, "inca_prepare (records)");
+  }
   cleanup();
-  tmp.release();
-  if (e != cudaSuccess) return cuda_error(c, e, "inca_prepare (records)");
   c->counts.read = n;
   c->counts.after_screen1 = static_cast<int64_t>(h_n1);
   c->counts.after_screen2 = nsurv;
