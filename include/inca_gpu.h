@@ -87,7 +87,10 @@ int inca_gen_closed_shell_dm2(inca_ctx* ctx, const double* D, int unique, int64_
  * JA8/polycoef of src/mod_intrastuff.f90:32-194): normalisation (normalize != 0, as
  * calculate_intracule(.true.)), screen 1, Gaussian products, the three polynomial
  * coefficient vectors (LU with partial pivoting), screen 2. lim = thresh/(nprim(nprim+1)/2).
- * The survivors stay resident on the device, grouped by angular class. counts may be NULL. */
+ * The survivors stay resident on the device, grouped by angular class. counts may be NULL.
+ * Device memory: for lists of up to 2^26 quartets the context keeps the call's sort scratch
+ * (about 24 B per quartet plus the radix sort's temporary storage) until inca_ctx_destroy, so
+ * a repeated preparation allocates nothing; larger lists give it back before returning. */
 int inca_prepare(inca_ctx* ctx, double thresh, int normalize, inca_counts* counts);
 
 /* Per-quartet screening results of the last inca_prepare, in input order (for checks):
