@@ -7,7 +7,7 @@ INCA uses them through ``LD0006`` ... ``LD5810`` (src/lebedev.f, ``gen_oh`` at l
 
 This script reads the same published literals from SciPy's independent distribution of the
 rules (``scipy.integrate._lebedev.get_lebedev_sphere``) and writes them as a C table. The
-orbit expansion itself is written in ``grid_tables.cpp``. Run it from the repository root:
+orbit expansion itself is written in ``host_tables.cpp``. Run it from the repository root:
 
     python inca_parallel_gb300/csrc/gen_lebedev.py
 

@@ -2,10 +2,10 @@
 // caller-owned device records into a caller-owned device output, allocating nothing.
 //
 // The context API (inca_eval) grows its own device buffers with cudaMalloc. Some callers
-// cannot allow that: code running inside a caller-managed memory pool or arena, a service
-// that must not allocate after start-up, or a host that records its own work for replay.
-// This entry point takes every input and output from the caller and keeps its only
-// intermediate (the per-split partial sums) in a fixed file-scope device array.
+// cannot allow that: code running inside a caller-managed memory pool or arena, or a service
+// that must not allocate after start-up so that it cannot run out of memory later. This entry
+// point takes every input and output from the caller and keeps its only intermediate (the
+// per-split partial sums) in a fixed file-scope device array.
 //
 // Work decomposition: a CTA owns 256 points (2 per thread) and one contiguous range of
 // records (its split); it writes one partial per point into the fixed scratch array, and a
@@ -15,6 +15,8 @@
 // threads) share the scratch array and race.
 #include <algorithm>
 #include <mutex>
+
+#include <cuda.h>  // driver API types only: the two functions used are resolved at run time
 
 #include "inca_internal.h"
 
@@ -29,14 +31,22 @@ constexpr int kTile = kThreads * kPPT;
 constexpr int kMaxDevices = 256;
 constexpr int kCoef = INCA_MAX_DEGREE + 1;
 
-// Per-device set-up, done once with that device current.
+// Per-device set-up, done with that device current, once per CUDA context: the scratch
+// array's address belongs to the context that loaded the module, so a context created anew
+// on the device (after cudaDeviceReset, or a caller's own context) is set up again.
 struct DeviceSlot {
   bool ready = false;
+  unsigned long long ctx_id = 0;
   double* scratch = nullptr;
   int num_sms = 0;
 };
 std::mutex g_setup_mutex;
 DeviceSlot g_slots[kMaxDevices];
+
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
 
 __global__ void __launch_bounds__(kThreads)
 k_eval_records(int64_t nrec, int64_t per_split, const double* __restrict__ A,
@@ -94,18 +104,46 @@ __global__ void k_sum_record_splits(const double* __restrict__ partial, int nspl
   out[g] = s;
 }
 
-// First call on a device: resolve the scratch array's address and the SM count.
+// Id of the calling thread's current CUDA context (0: none is current yet). Ids are unique
+// for the life of the process, so a context created after a reset has a new one.
+int current_ctx_id(unsigned long long* id) {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return INCA_E_CUDA;
+    g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+    g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f2);
+  }
+  CUcontext c = nullptr;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS) return INCA_E_CUDA;
+  *id = 0;
+  if (c && g_ctx_get_id(c, id) != CUDA_SUCCESS) return INCA_E_CUDA;
+  return INCA_OK;
+}
+
+// Set-up of a device for the current context: resolve the scratch array's address and the
+// SM count (first call on the device, and again whenever the current context has changed).
 int device_setup(int dev, DeviceSlot* out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
+  unsigned long long id = 0;
+  int st = current_ctx_id(&id);
+  if (st != INCA_OK) return st;
   DeviceSlot& s = g_slots[dev];
-  if (!s.ready) {
+  if (!s.ready || id == 0 || s.ctx_id != id) {
     void* p = nullptr;
+    // with no context current yet, this call also initialises the device's primary context
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return INCA_E_CUDA;
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return INCA_E_CUDA;
+    if (id == 0 && ((st = current_ctx_id(&id)) != INCA_OK || id == 0)) return st != INCA_OK ? st : INCA_E_CUDA;
     s.scratch = static_cast<double*>(p);
     s.num_sms = sms;
+    s.ctx_id = id;
     s.ready = true;
   }
   *out = s;
@@ -125,6 +163,9 @@ extern "C" int inca_eval_records_noalloc(int64_t nrec, const double* A, const do
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return INCA_E_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return INCA_E_LIMIT;
+  // an error left pending by the caller's own work is reported, not cleared, and nothing is
+  // queued (otherwise the launch checks below would take it for a failure of this call)
+  if (cudaPeekAtLastError() != cudaSuccess) return INCA_E_CUDA;
   DeviceSlot slot;
   const int st = device_setup(dev, &slot);
   if (st != INCA_OK) return st;

@@ -264,10 +264,9 @@ int inca_mlp_train(inca_mlp* mlp, int64_t n, const float* X, const float* T, int
  * Evaluation without allocation. No counterpart in the reference (the Fortran program
  * allocates its work arrays itself); this entry point exists for callers that must not
  * allocate device memory while they run: a solver that keeps all its device memory in its
- * own pool or arena, a long-running service that allocates only at start-up so that it
- * can never fail for lack of memory later, or a host that records its GPU work for replay.
- * The context API above cannot serve them, because inca_eval grows its buffers with
- * cudaMalloc.
+ * own pool or arena, or a long-running service that allocates only at start-up so that it
+ * can never fail for lack of memory later. The context API above cannot serve them, because
+ * inca_eval grows its buffers with cudaMalloc.
  *
  * Computes ivec[g] = sum_q A[q] exp(-|r'|^2) Vx(r'_x) Vy(r'_y) Vz(r'_z),
  * r' = sqe[q] (r_g + d_q), in FP64, for nrec survivor records laid out as inca_get_records
@@ -282,11 +281,15 @@ int inca_mlp_train(inca_mlp* mlp, int64_t n, const float* X, const float* T, int
  *  - npts <= INCA_NOALLOC_MAX_POINTS; a larger npts returns INCA_E_LIMIT and queues nothing.
  *    The intermediate sums live in a fixed 16 MiB device array inside the library.
  *  - The first call on a device sets that device up (it looks up the address of the fixed
- *    array); make that first call before any stream capture begins.
+ *    array in the current CUDA context); make that first call before any stream capture
+ *    begins. A call made under a different context than the last one on that device (for
+ *    instance after cudaDeviceReset) sets the device up again, and the same rule applies.
  *  - Calls that overlap in time on one device (different streams or host threads) share the
  *    fixed array and race: order them, e.g. on one stream.
+ *  - nrec == 0 writes zeros to ivec with one cudaMemsetAsync on `stream`.
  *  - Status codes only (there is no context for inca_last_error): INCA_E_ARG for negative
- *    sizes or null pointers, INCA_E_LIMIT as above, INCA_E_CUDA for a launch failure.
+ *    sizes or null pointers, INCA_E_LIMIT as above, INCA_E_CUDA for a launch failure or for
+ *    a CUDA error already pending on the calling thread (left pending; nothing is queued).
  */
 #define INCA_NOALLOC_MAX_POINTS (1 << 21)
 int inca_eval_records_noalloc(int64_t nrec, const double* A, const double* sqe,

@@ -95,3 +95,19 @@ def test_noalloc_limits_and_empty(env):
                                          pts.data_ptr(), out.data_ptr(), s) == INCA_OK
     torch.cuda.synchronize()
     assert out.cpu().numpy().tolist() == [0.0] * 4
+
+
+def test_noalloc_empty_records_on_side_stream(env):
+    """nrec == 0 queues one memset of the output on the caller's (non-default) stream."""
+    ctx, lib, torch = env
+    side = torch.cuda.Stream()
+    out = torch.full((1000,), float("nan"), dtype=torch.float64, device="cuda")
+    pts = torch.zeros(3000, dtype=torch.float64, device="cuda")
+    null = ctypes.c_void_p(0)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        assert lib.inca_eval_records_noalloc(0, null, null, null, null, null, 1000, pts.data_ptr(),
+                                             out.data_ptr(), ctypes.c_void_p(side.cuda_stream)) == INCA_OK
+    side.synchronize()
+    assert not np.isnan(out.cpu().numpy()).any()
+    assert np.all(out.cpu().numpy() == 0.0)
