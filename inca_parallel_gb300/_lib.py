@@ -45,6 +45,8 @@ SIGNATURES = {
     "inca_set_primitives": (ctypes.c_int, [VP, ctypes.c_int32, DP, IP, DP, DP, DP]),
     "inca_load_dm2p": (ctypes.c_int, [VP, ctypes.c_char_p, I64P]),
     "inca_set_quartets": (ctypes.c_int, [VP, ctypes.c_int64, IP, DP]),
+    "inca_read_dm2p": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int64, IP, DP, I64P, ctypes.c_char_p,
+                                      ctypes.c_int32]),
     "inca_gen_closed_shell_dm2": (ctypes.c_int, [VP, DP, ctypes.c_int, I64P]),
     "inca_prepare": (ctypes.c_int, [VP, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Counts)]),
     "inca_get_screening": (ctypes.c_int, [VP, U8P, DP, DP]),
@@ -63,6 +65,7 @@ SIGNATURES = {
     "inca_last_eval_stats": (ctypes.c_int, [VP, I64P, I64P, I64P, I64P]),
     "inca_get_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
     "inca_last_eval_phases": (ctypes.c_int, [VP, DP, DP]),
+    "inca_last_eval_cheap_pairs": (ctypes.c_int, [VP, I64P]),
     "inca_kernel_launches": (ctypes.c_int, [VP, I64P]),
     "inca_fp32_fma_peak": (ctypes.c_int, [VP, DP]),
     "inca_mlp_create": (ctypes.c_int, [ctypes.POINTER(VP), ctypes.c_int, ctypes.c_int32, ctypes.c_int32,
@@ -368,7 +371,10 @@ class Context:
         a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         self._check(self.lib.inca_last_eval_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                                   ctypes.byref(d)))
-        return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value, "corrected_terms": d.value}
+        e = ctypes.c_int64()
+        self._check(self.lib.inca_last_eval_cheap_pairs(self.h, ctypes.byref(e)))
+        return {"fp32_pairs": a.value, "precise_pairs": b.value, "skipped_pairs": c.value, "corrected_terms": d.value,
+                "cheap_pairs": e.value}
 
     def fp32_peak_tflops(self):
         """Measured FP32 FMA throughput of the context's GPU (TFLOP/s)."""
@@ -380,6 +386,23 @@ class Context:
         a, b = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.inca_last_eval_phases(self.h, ctypes.byref(a), ctypes.byref(b)))
         return {"pass1_ms": a.value, "pass2_ms": b.value}
+
+
+def read_dm2p(path, nprim):
+    """The library's .dm2p reader on the host (no device): (ijkl (n,4) int32 1-based, v (n,)).
+    Raises IncaError with the library's status and message."""
+    lib = load()
+    n = ctypes.c_int64()
+    err = ctypes.create_string_buffer(512)
+    st = lib.inca_read_dm2p(os.fsencode(path), int(nprim), 0, None, None, ctypes.byref(n), err, 512)
+    if st:
+        raise IncaError(st, err.value.decode(errors="replace"))
+    ijkl = np.zeros((n.value, 4), dtype=np.int32)
+    v = np.zeros(n.value)
+    st = lib.inca_read_dm2p(os.fsencode(path), int(nprim), n.value, _i(ijkl), _d(v), ctypes.byref(n), err, 512)
+    if st:
+        raise IncaError(st, err.value.decode(errors="replace"))
+    return ijkl, v
 
 
 def centercalc(an, cartes, nohydro=True, betaone=False):

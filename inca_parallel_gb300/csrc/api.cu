@@ -204,6 +204,30 @@ int inca_load_dm2p(inca_ctx* c, const char* path, int64_t* nread) {
   return upload_quartets(c, static_cast<int64_t>(v.size()), reinterpret_cast<const int32_t*>(q.data()), v.data());
 }
 
+int inca_read_dm2p(const char* path, int32_t nprim, int64_t capacity, int32_t* ijkl, double* v, int64_t* nread,
+                   char* errbuf, int32_t errlen) {
+  if (errbuf && errlen > 0) errbuf[0] = '\0';
+  if (!path || nprim <= 0 || capacity < 0 || !nread) return INCA_E_ARG;
+  std::vector<int4> q;
+  std::vector<double> vv;
+  std::string err;
+  const int st = read_dm2p(path, nprim, q, vv, err);
+  if (st) {
+    if (errbuf && errlen > 0) {
+      std::strncpy(errbuf, err.c_str(), static_cast<size_t>(errlen) - 1);
+      errbuf[errlen - 1] = '\0';
+    }
+    return st;
+  }
+  const int64_t n = static_cast<int64_t>(vv.size());
+  *nread = n;
+  if (!ijkl || !v) return INCA_OK;  // count only
+  if (n > capacity) return INCA_E_LIMIT;
+  std::memcpy(ijkl, q.data(), sizeof(int4) * static_cast<size_t>(n));
+  std::memcpy(v, vv.data(), sizeof(double) * static_cast<size_t>(n));
+  return INCA_OK;
+}
+
 int inca_set_quartets(inca_ctx* c, int64_t n, const int32_t* ijkl, const double* v) {
   CTX_CHECK(c);
   if (n < 0 || (n > 0 && (!ijkl || !v))) return set_error(c, INCA_E_ARG, "inca_set_quartets: bad arguments");
@@ -448,6 +472,12 @@ int inca_last_eval_stats(inca_ctx* c, int64_t* fp32_pairs, int64_t* precise_pair
   if (precise_pairs) *precise_pairs = c->pairs_fp64;
   if (skipped_pairs) *skipped_pairs = c->pairs_skip;
   if (corrected_terms) *corrected_terms = c->corrected_points;
+  return INCA_OK;
+}
+
+int inca_last_eval_cheap_pairs(inca_ctx* c, int64_t* cheap_pairs) {
+  if (!c) return INCA_E_ARG;
+  if (cheap_pairs) *cheap_pairs = c->pairs_cheap;
   return INCA_OK;
 }
 

@@ -445,6 +445,7 @@ int eval_cube_separable(inca_ctx* c, double eps) {
   c->pairs_fp64 = static_cast<int64_t>(run.live);  // (record, tile) pairs evaluated in double-float
   c->pairs_skip = static_cast<int64_t>(run.skip);
   c->corrected_points = 0;
+  c->pairs_cheap = 0;
   return INCA_OK;
 }
 

@@ -221,7 +221,7 @@ struct inca_ctx {
   // timing and tier statistics of the last evaluation
   double t_total_ms = 0, t_kernel_ms = 0, t_pass2_ms = 0;
   int t_kernel_launches = 0, t_launches = 0;
-  int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0, corrected_points = 0;
+  int64_t pairs_fp32 = 0, pairs_fp64 = 0, pairs_skip = 0, corrected_points = 0, pairs_cheap = 0;
   int64_t launches = 0;  // own kernel launches since creation
 
   // schedule of the mixed evaluation (inca_autotune / inca_set_tuning; 0 or < 0: defaults)

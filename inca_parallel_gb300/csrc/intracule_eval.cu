@@ -107,7 +107,7 @@ int eval_device(inca_ctx* c, int mode, double tol, bool graph) {
   if (c->d_ivec.reserve(c->ngrid)) return set_error(c, INCA_E_NOMEM, "ivec");
   c->t_total_ms = c->t_kernel_ms = c->t_pass2_ms = 0;
   c->t_kernel_launches = c->t_launches = 0;
-  c->pairs_fp32 = c->pairs_fp64 = c->pairs_skip = c->corrected_points = 0;
+  c->pairs_fp32 = c->pairs_fp64 = c->pairs_skip = c->corrected_points = c->pairs_cheap = 0;
   if (mode == INCA_MIXED) {
     const int st = graph ? eval_mixed_graph(c, tol > 0 ? tol : 1e-10) : eval_mixed(c, tol > 0 ? tol : 1e-10);
     if (st == INCA_OK) c->evaluated = true;

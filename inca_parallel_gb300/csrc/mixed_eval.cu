@@ -235,6 +235,110 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
   for (int p = 0; p < NP; ++p) t[p] = __fmaf_rn(E[p], A_hi, __fmul_rn(E[p], A_lo));
 }
 
+// ---------------------------------------------------------------- cheap tier (one-pass form)
+// A (record, tile) pair whose terms are all small next to the tile's drop threshold is
+// evaluated in plain FP32: u_d = fma(s_hi, x_d, b_hi) from the point rounded to nearest,
+// the hardware ex2.approx, the FP32 coefficients and an FP32 sum over the chunk. Instead of
+// entering the statistical error model, each such term carries a rigorous bound of its error,
+// c 2^lb (2^lb bounds |term| over the tile), which is added to the tile's left-out bound mass
+// like a dropped term's 2^lb: the pair qualifies when c 2^lb is at most the drop threshold.
+//
+// The bound, with u = 2^-24, K_d = 2 s X_d + |b_d| (X_d: largest |x_d| over the tile box) and
+// m_d / M_d the smallest / largest |u_d| over the box (as in log2_bound):
+//  * |u^_d - u_d| <= D_d = u (K_d + |u_d|)  (s, b and x each rounded once, then the FMA);
+//  * y = -|u|^2 in three roundings: |y^ - y| <= sum_d 2 |u_d| D_d + 3 u |u|^2 (+ D_d^2);
+//    2^-|u|^2 |u_d| <= 2^-sum m^2 max(m_d, 1/sqrt(2 ln 2)) and 2^-S S <= 2^-sum m^2
+//    max(sum m^2, 1/ln 2), so E |y^ - y| ln 2 <= 2^-sum m^2 u ln2 (2 sum_d K_d max(m_d, 0.8494)
+//    + 5 max(sum m^2, 1.4427));
+//  * ex2.approx.ftz.f32: relative error at most kEx2RelErr over [-126, 0] (measured against
+//    exp2 in FP64 over every FP32 argument there on a GB300: largest 2.42 u, mean -0.07 u), and
+//    a result below 2^-126 flushed to zero: at most 2^(sum m^2 - 126) of 2^lb;
+//  * Horner in FP32 with FP32 coefficients: (2 L_d + 1) u of P_d(M_d), and the error of u^_d
+//    through V_d': L_d D_d of P_d(M_d);
+//  * four products and the FP32 mantissa of A': 5 u; the FP32 sum of at most 32 terms: 31 u.
+// Pairs qualify only where the argument bounds keep every piece small: |u_d| < kFastU (the
+// polynomials cannot overflow), K_d <= 80 (so D_d stays inside the 1e-5 widening of the box
+// bounds of log2_bound), and |ks| <= 100 (A' = m 2^ks is a normal FP32 number). Explicit
+// round-to-nearest intrinsics: the one-pass kernel and the correction pass take the same
+// decision from the same record, box and threshold.
+constexpr float kEx2RelErr = 2.5f * 5.9604645e-08f;
+constexpr float kCheapKMax = 80.0f;
+constexpr int kCheapKsMax = 100;
+
+// log2 of the cheap tier's error bound for record R over the tile box, or +inf when the pair
+// does not qualify. lb: the pair's log2_bound over the same box.
+__device__ __forceinline__ float cheap_log2_err(const float* __restrict__ R, const int L[3], const float* box,
+                                                float lb) {
+  const float s = R[0];
+  const float ks = R[11];
+  bool ok = ks >= -static_cast<float>(kCheapKsMax) && ks <= static_cast<float>(kCheapKsMax);
+  float S = 0.0f, kt = 0.0f, vp = 0.0f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float b = R[2 + d];
+    const float a0 = __fmaf_rn(s, box[d], b), a1 = __fmaf_rn(s, box[3 + d], b);
+    float m = (a0 <= 0.0f && a1 >= 0.0f) ? 0.0f : fminf(fabsf(a0), fabsf(a1));
+    float M = fmaxf(fabsf(a0), fabsf(a1));
+    m = fmaxf(0.0f, __fsub_rn(__fmul_rn(m, 1.0f - 1e-5f), 1e-5f));
+    M = __fadd_rn(__fmul_rn(M, 1.0f + 1e-5f), 1e-5f);
+    const float X = fmaxf(fabsf(box[d]), fabsf(box[3 + d]));
+    const float K = __fmaf_rn(__fmul_rn(2.0f, s), X, fabsf(b));
+    ok = ok && K <= kCheapKMax && M < kFastU;
+    S = __fmaf_rn(m, m, S);
+    kt = __fmaf_rn(K, fmaxf(m, 0.8494f), kt);
+    const float Lf = static_cast<float>(L[d]);
+    vp = __fadd_rn(vp, __fmaf_rn(Lf, __fadd_rn(K, M), __fmaf_rn(2.0f, Lf, 1.0f)));
+  }
+  // c / u, with margins of 1 % (first-order expansions; every piece is below 1e-3 here)
+  float cu = __fmul_rn(0.7002f, __fmaf_rn(2.0f, kt, __fmul_rn(5.0f, fmaxf(S, 1.4427f))));
+  cu = __fadd_rn(cu, __fadd_rn(__fmul_rn(1.01f, vp), 36.0f + kEx2RelErr / 5.9604645e-08f));
+  const float c = __fadd_rn(__fmul_rn(__fmul_rn(cu, 1.0001f), 5.9604645e-08f), exp2f(__fsub_rn(S, 125.99f)));
+  return ok ? __fadd_rn(lb, __fadd_rn(__log2f(c), 0.02f)) : HUGE_VALF;
+}
+
+__device__ __forceinline__ float ex2_approx(float y) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+
+// Cheap-tier terms of record R at NP points (rn: the points rounded to nearest), added to sc.
+template <int NP>
+__device__ __forceinline__ void terms_cheap(const float* __restrict__ R, const int L[3], const float (&rn)[3][NP],
+                                            float (&sc)[NP]) {
+  const float4 R0 = *reinterpret_cast<const float4*>(R);
+  const float4 R1 = *reinterpret_cast<const float4*>(R + 4);
+  const float4 R2 = *reinterpret_cast<const float4*>(R + 8);
+  const float s = R0.x;
+  const float bh[3] = {R0.z, R0.w, R1.x};
+  // A' = m 2^ks as one FP32 number (|ks| <= 100 for this tier)
+  const float A = __fmul_rn(R2.x, __int_as_float((static_cast<int>(R2.w) + 127) << 23));
+  float u[3][NP], E[NP];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) u[d][p] = __fmaf_rn(s, rn[d][p], bh[d]);
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    float y = __fmul_rn(-u[0][p], u[0][p]);
+    y = __fmaf_rn(-u[1][p], u[1][p], y);
+    y = __fmaf_rn(-u[2][p], u[2][p], y);
+    E[p] = ex2_approx(y);
+  }
+  const float* Cx = R + 12;
+  const float* Cd[3] = {Cx, Cx + L[0] + 1, Cx + L[0] + L[1] + 2};
+  float v[NP], a[NP];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (L[d]) {
+      poly2_pts<NP, false>(L[d], Cd[d], u[d], v, a);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) E[p] = __fmul_rn(E[p], v[p]);
+    }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) sc[p] = __fmaf_rn(E[p], A, sc[p]);
+}
+
 // The same FP32 term and error bound for one point with loop-based Horner (compact code for
 // the correction pass; same operation sequence and rounding as terms32).
 __device__ __noinline__ void term32_one(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry,
@@ -394,10 +498,15 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
         int64_t nitems, int stage_floats, const float* __restrict__ pt_tau,
-        const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop, double* __restrict__ part,
-        double* __restrict__ part_abs, double* __restrict__ drop_mass, unsigned long long* __restrict__ work,
-        unsigned long long* __restrict__ stats, int* __restrict__ err) {
+        const float2* __restrict__ exp_tab, const float* __restrict__ lt_drop, int cheap_tier,
+        double* __restrict__ part, double* __restrict__ part_abs, double* __restrict__ drop_mass,
+        unsigned long long* __restrict__ work, unsigned long long* __restrict__ stats, int* __restrict__ err,
+        int wait_test) {
   static_assert(!(kFuse && kEst), "the estimate pass has no corrections");
+  // wait_test > 0 (a test of the bounded waits, never in production): no staging copy is
+  // started and every wait gives up after wait_test tries, so the error path runs
+  const bool issue = wait_test == 0;
+  const int wlim = wait_test > 0 ? wait_test : kWaitLimit;
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
@@ -408,7 +517,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
   if (kFuse)
     for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
   stage_init(S);
-  unsigned long long nskip = 0, nlive = 0, ncorr = 0, nround = 0;
+  unsigned long long nskip = 0, nlive = 0, ncorr = 0, nround = 0, ncheap = 0;
   int k = 0;  // chunks taken by this CTA so far: selects buffer and barrier phase
   for (;;) {
     const int64_t item = next_item(work);
@@ -429,7 +538,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       dat = W.doff + static_cast<int64_t>(split) * W.ntiles + tl;
     }
     const TileInfo T = tiles[wtile];
-    if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
+    if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first, issue);
     float rh[3][kPPT], rl[3][kPPT];
     load_points(phi, plo, T, lane, rh, rl);
     float tau[kPPT];
@@ -458,7 +567,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     int nfold = 0;
     bool ok = true;
     for (int ch = first; ch < cr.end; ch += nsplit, ++k) {
-      ok = __all_sync(0xffffffffu, stage_next(S, chunks, segs, rec32, k, ch + nsplit, cr.end));
+      ok = __all_sync(0xffffffffu, stage_next(S, chunks, segs, rec32, k, ch + nsplit, cr.end, wlim, issue));
       if (!ok) break;
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
@@ -471,14 +580,47 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       const int rs = __reduce_max_sync(0xffffffffu, sg.stride32);
       float umax = HUGE_VALF;
       const float lb = lane < w.count ? log2_bound(st + lane * rs, L, box, nullptr, &umax) : -HUGE_VALF;
-      uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      const bool live = lane < w.count && lb > thr;
+      // cheap tier (one-pass form with dropping): pairs whose rigorous FP32 error bound stays
+      // within the drop threshold; the bound joins the left-out mass
+      uint32_t mc = 0u;
+      if (kFuse && lt_drop && cheap_tier) {
+        const float lc = live ? cheap_log2_err(st + lane * rs, L, box, lb) : HUGE_VALF;
+        const bool cheap = lc <= thr;
+        mc = __ballot_sync(0xffffffffu, cheap);
+        if (cheap) dm += exp2f(lc);
+      }
+      uint32_t m = __ballot_sync(0xffffffffu, live) & ~mc;
       const uint32_t fast = INCA_FAST_TERMS ? __ballot_sync(0xffffffffu, lane < w.count && umax < kFastU &&
                                                                            st[lane * rs + 11] <= 100.0f)
                                             : 0u;
       if (kFuse && lane < w.count && !(lb > thr)) dm += exp2f(lb);
       if (lane == 0) {
-        nskip += w.count - __popc(m);
+        nskip += w.count - __popc(m) - __popc(mc);
         nlive += __popc(m);
+        ncheap += __popc(mc);
+      }
+      if (kFuse && mc) {
+        // the points rounded to nearest (the cheap terms' coordinates), once per chunk
+        float rn[3][kPPT], sc[kPPT];
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d) rn[d][p] = __fadd_rn(rh[d][p], rl[d][p]);
+          sc[p] = 0.0f;
+        }
+        uint32_t mm = mc;
+        while (mm) {
+          const int q = __ffs(mm) - 1;
+          mm &= mm - 1;
+          terms_cheap<kPPT>(st + q * rs, L, rn, sc);
+        }
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) {
+          const f2 s2 = two_sum(sh[p], sc[p]);
+          sh[p] = s2.hi;
+          sl[p] = __fadd_rn(sl[p], s2.lo);
+        }
       }
       uint32_t nm[kPPT];
 #pragma unroll
@@ -609,6 +751,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       atomicAdd(&stats[0], nlive);
       atomicAdd(&stats[1], nround);
       atomicAdd(&stats[3], ncorr);
+      atomicAdd(&stats[13], ncheap);
     }
   }
 }
@@ -619,8 +762,8 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
         const float* __restrict__ gbox, const float* __restrict__ g_lt, const float* __restrict__ pt_tau,
-        const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop, const float2* __restrict__ exp_tab,
-        int64_t nitems, int stage_floats, double* __restrict__ part,
+        const float* __restrict__ pt_tau_est, const float* __restrict__ lt_drop, int cheap_tier,
+        const float2* __restrict__ exp_tab, int64_t nitems, int stage_floats, double* __restrict__ part,
         unsigned long long* __restrict__ work, unsigned long long* __restrict__ stats, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
@@ -685,14 +828,18 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       const float* Rq = st + lane * sg.stride32;
       // the skip decision of the pass over all terms (same box, arithmetic and threshold)
       const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
-      const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      // pairs of the one-pass kernel's cheap tier (same decision): their error is bounded
+      // within the left-out mass, nothing to correct
+      const bool cheap =
+          lt_drop && cheap_tier && lane < w.count && lb > thr && cheap_log2_err(Rq, L, wbox, lb) <= thr;
+      const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr && !cheap);
       uint32_t msub[kPPT];
       uint32_t any = 0;
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
         float lerr = -HUGE_VALF;
         if (lane < w.count) log2_bound(Rq, L, gbox + (wtile * kPPT + p) * 8, &lerr);
-        msub[p] = __ballot_sync(0xffffffffu, lane < w.count && lerr > g_lt[wtile * kPPT + p]);
+        msub[p] = __ballot_sync(0xffffffffu, lane < w.count && !cheap && lerr > g_lt[wtile * kPPT + p]);
         any |= msub[p];
       }
       if (lane == 0) {
@@ -1291,7 +1438,7 @@ double env_knob(const char* name, double dflt, double lo, double hi) {
 // context's scratch) and uploaded tables. The launch sequence then runs on the device alone.
 struct MixedPlan {
   bool fused = false;
-  int mode = 2, nseg = 1, emode = 0, nmol = 1;
+  int mode = 2, nseg = 1, emode = 0, nmol = 1, cheap = 1, wait_test = 0;
   const int* seg_of = nullptr;
   int64_t ngrid = 0, nwt = 0, ngroups = 0, nitems = 0, npart = 0, ndrop = 0;
   int64_t ns = 0, nitems_s = 0, npart_s = 0;
@@ -1322,6 +1469,11 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   P.tau_scale = env_knob("INCA_TAU_SCALE", kTauScale, 1e-300, HUGE_VAL);
   P.drop_frac = env_knob("INCA_DROP_FRACTION", c->tune_drop >= 0.0 ? c->tune_drop : kDropFrac, 0.0, 0.5);
   P.safety = env_knob("INCA_EST_SAFETY", c->tune_safety >= 0.0 ? c->tune_safety : kEstSafety, 0.0, HUGE_VAL);
+  // the cheap tier of the one-pass form (0 evaluates every live pair in compensated FP32)
+  P.cheap = env_knob("INCA_CHEAP_TIER", 1.0, 0.0, 2.0) >= 0.5 ? 1 : 0;
+  // test of the bounded staging waits: the pass-1 kernels start no copy and give up waiting
+  // after this many tries (0: off)
+  P.wait_test = static_cast<int>(env_knob("INCA_TEST_STAGE_TIMEOUT", 0.0, 0.0, 1e6));
   P.nwt = c->ntiles;
   P.ngroups = P.nwt * kPPT;
   const int ipc = c->tune_items_per_cta > 0 ? c->tune_items_per_cta : kItemsPerCta;
@@ -1451,7 +1603,7 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
     INCA_LAUNCH(c, (k_pass1<false, true>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p,
                 c->d_rec32.p,
                 c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, P.nitems_s, P.stage_floats, nullptr,
-                nullptr, nullptr, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw);
+                nullptr, nullptr, 0, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw, P.wait_test);
     INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
     INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.qabs, nullptr, P.Mss);
     if (P.mode == 0) {
@@ -1484,11 +1636,11 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   if (P.fused)
     INCA_LAUNCH(c, k_pass1<true>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,
-                use_drop ? P.ltdrop : nullptr, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw);
+                use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw, P.wait_test);
   else
     INCA_LAUNCH(c, k_pass1<false>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,
                 c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
-                nullptr, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw);
+                nullptr, 0, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw, P.wait_test);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[2], c->stream));
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
@@ -1525,7 +1677,8 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[3], c->stream));
   INCA_LAUNCH(c, k_pass2, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
               c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
-              use_drop ? P.ltdrop : nullptr, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1, P.stats + 4, P.errw);
+              use_drop ? P.ltdrop : nullptr, P.cheap, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1, P.stats + 4,
+              P.errw);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[4], c->stream));
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, P.p2, P.Is);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, c->d_ivec.p);
@@ -1562,7 +1715,9 @@ int mixed_finish(inca_ctx* c, const MixedPlan& P, Events* ev, bool* retry) {
     c->pairs_fp64 = static_cast<int64_t>(hs[1]) + static_cast<int64_t>(hs[5]);
     c->pairs_skip = static_cast<int64_t>(hs[2]);
     c->corrected_points = static_cast<int64_t>(hs[3]) + 32 * static_cast<int64_t>(hs[7]);
+    c->pairs_cheap = static_cast<int64_t>(hs[13]);
   } else {
+    c->pairs_cheap = 0;
     c->pairs_fp32 = static_cast<int64_t>(hs[4]);
     c->pairs_fp64 = static_cast<int64_t>(hs[5]);
     c->pairs_skip = static_cast<int64_t>(hs[2]);
@@ -1690,6 +1845,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
 static std::vector<double> plan_signature(const inca_ctx* c, const MixedPlan& P) {
   auto a = [](const void* p) { return static_cast<double>(reinterpret_cast<uintptr_t>(p)); };
   std::vector<double> s = {double(P.fused), double(P.mode), double(P.nseg), double(P.emode), double(P.nmol),
+                           double(P.cheap), double(P.wait_test),
                            a(P.seg_of), double(P.ngrid), double(P.nwt), double(P.ngroups), double(P.nitems),
                            double(P.npart), double(P.ndrop), double(P.ns), double(P.nitems_s), double(P.npart_s),
                            double(P.nctas), double(P.nctas_s), double(P.gblk), double(P.tblk),

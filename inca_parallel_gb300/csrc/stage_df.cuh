@@ -43,8 +43,8 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       : "memory");
 }
 // Bounded wait for the barrier phase with the given parity; false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < kWaitLimit; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kWaitLimit) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -97,9 +97,11 @@ __device__ __forceinline__ void stage_init(const Stage& S) {
 }
 
 // Start the copy of an item's first chunk (global chunk counter k) into buffer k & 1.
+// issue = false (test of the bounded waits only): no copy is started, so the wait on that
+// buffer runs out.
 __device__ __forceinline__ void stage_first(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
-                                            const float* rec32, int k, int ch) {
-  if (threadIdx.x == 0) {
+                                            const float* rec32, int k, int ch, bool issue = true) {
+  if (threadIdx.x == 0 && issue) {
     fence_proxy_async();  // earlier generic-proxy reads of that buffer are done (warp-synchronous)
     const ChunkRef r = chunk_ref(chunks, segs, rec32, ch);
     bulk_load(S.buf(k), r.src, r.bytes, &S.bar[k & 1]);
@@ -143,15 +145,17 @@ __device__ __forceinline__ int64_t next_item(unsigned long long* work) {
 // Before working on chunk k: start the copy of the next chunk into the other buffer, then wait
 // for this one. Returns false if the wait gave up; the other buffer's copy (if started) is then
 // drained, again with a bounded wait, so no copy is left in flight when the CTA exits.
+// limit / issue: the wait limit, and whether copies are started (see stage_first).
 __device__ __forceinline__ bool stage_next(const Stage& S, const WorkChunk* chunks, const ClassSeg* segs,
-                                           const float* rec32, int k, int next, int nchunks) {
-  if (threadIdx.x == 0 && next < nchunks) {
+                                           const float* rec32, int k, int next, int nchunks,
+                                           int limit = kWaitLimit, bool issue = true) {
+  if (threadIdx.x == 0 && next < nchunks && issue) {
     fence_proxy_async();  // the generic-proxy reads of that buffer (chunk k-1) are done
     const ChunkRef r = chunk_ref(chunks, segs, rec32, next);
     bulk_load(S.buf(k + 1), r.src, r.bytes, &S.bar[(k + 1) & 1]);
   }
-  if (mbar_wait(&S.bar[k & 1], static_cast<uint32_t>((k >> 1) & 1))) return true;
-  if (next < nchunks) mbar_wait(&S.bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1));
+  if (mbar_wait(&S.bar[k & 1], static_cast<uint32_t>((k >> 1) & 1), limit)) return true;
+  if (next < nchunks) mbar_wait(&S.bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1), limit);
   return false;
 }
 

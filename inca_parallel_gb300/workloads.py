@@ -14,6 +14,8 @@ Workloads (seed = 20261203 + index):
      exponents log-uniform in [0.1, 5000], 21 occupied orbitals.
   3  molecules of 3..20 atoms at random non-overlapping positions (>= 1.8 bohr apart),
      20..300 primitives l<=2.
+  4  a 20-atom molecule of that kind with about 300 primitives (exponents up to 200) and 60
+     occupied orbitals, for the vector cube.
 """
 import math
 
@@ -148,7 +150,7 @@ def ring_molecule(seed=SEED0 + 2, nprim_target=200):
     return _basis(atoms, prims)
 
 
-def random_molecule(rng, natoms, nprim_target, mind=1.8):
+def random_molecule(rng, natoms, nprim_target, mind=1.8, hi=5000.0):
     pos = []
     while len(pos) < natoms:
         p = rng.uniform(-0.9, 0.9, size=3) * (2.0 + natoms ** (1 / 3) * 1.6)
@@ -159,8 +161,30 @@ def random_molecule(rng, natoms, nprim_target, mind=1.8):
     atoms, prims = [], []
     for z, p in zip(zs, pos):
         atoms.append((z, tuple(p)))
-        prims += [(a, c, tuple(p)) for a, c in random_atom_basis(rng, per, lmax=2 if z > 1 else 1)]
+        prims += [(a, c, tuple(p)) for a, c in random_atom_basis(rng, per, lmax=2 if z > 1 else 1, hi=hi)]
     return _basis(atoms, prims)
+
+
+def ring_workload(nprim_target=200, nocc=21):
+    """Workload 2: the 12-atom ring and its closed-shell 1-RDM (D, overlap)."""
+    b = ring_molecule(nprim_target=nprim_target)
+    D, S = closed_shell_density(b, nocc, SEED0 + 2)
+    return b, D
+
+
+def cube_molecule(seed=SEED0 + 4, natoms=20, nprim_target=300, hi=200.0):
+    """Workload 4 (cubeintra): a 20-atom molecule with about 300 primitives, l <= 2, exponents
+    log-uniform in [0.1, 200] (beyond a few hundred the reference's polynomial fit breaks down for
+    d shells on different atoms, so larger exponents would only test that breakdown)."""
+    rng = np.random.default_rng(seed)
+    return random_molecule(rng, natoms, nprim_target, hi=hi)
+
+
+def cube_workload(nocc=60):
+    """Workload 4: the 20-atom molecule and its closed-shell 1-RDM with 60 occupied orbitals."""
+    b = cube_molecule()
+    D, S = closed_shell_density(b, nocc, SEED0 + 4)
+    return b, D
 
 
 def electrons(basis):

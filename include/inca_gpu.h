@@ -74,6 +74,14 @@ int inca_set_primitives(inca_ctx* ctx, int32_t nprim, const double* alpha, const
  * Formats with 8-byte or zero markers fail with INCA_E_FORMAT. nread may be NULL. */
 int inca_load_dm2p(inca_ctx* ctx, const char* path, int64_t* nread);
 
+/* The same .dm2p read on the host alone, without a context or a device: the records go into the
+ * caller's arrays (ijkl[4*q+0..3], v[q]; at most `capacity` records, else INCA_E_LIMIT). With
+ * ijkl or v NULL only *nread is set. Status as for inca_load_dm2p; the message goes to errbuf
+ * (errlen bytes, NUL-terminated) when given. Replaces the same read as inca_load_dm2p
+ * (src/mod_intracule.f90:164-262), for hosts that inspect or filter the records themselves. */
+int inca_read_dm2p(const char* path, int32_t nprim, int64_t capacity, int32_t* ijkl, double* v, int64_t* nread,
+                   char* errbuf, int32_t errlen);
+
 /* Quartets from memory: ijkl[4*q+0..3] = i,j,k,l (1-based), v[q] = DM2 value. */
 int inca_set_quartets(inca_ctx* ctx, int64_t n, const int32_t* ijkl, const double* v);
 
@@ -199,6 +207,12 @@ int inca_last_eval_timing(inca_ctx* ctx, double* total_ms, double* kernel_ms,
  * of 32 points). The FP64 form reports zeros. Pointers may be NULL. */
 int inca_last_eval_stats(inca_ctx* ctx, int64_t* fp32_pairs, int64_t* precise_pairs,
                          int64_t* skipped_pairs, int64_t* corrected_terms);
+
+/* (Quartet, 128-point tile) pairs of the last INCA_MIXED evaluation that took the cheap tier of
+ * the one-pass form: plain FP32 terms whose rigorous error bound is counted with the terms left
+ * out, as a dropped term's bound is (0 for other forms; these pairs are not in fp32_pairs of
+ * inca_last_eval_stats). No counterpart in the reference. */
+int inca_last_eval_cheap_pairs(inca_ctx* ctx, int64_t* cheap_pairs);
 
 /* Device milliseconds of the two passes of the last INCA_MIXED evaluation (estimate pass over
  * all terms; correction pass). The FP64 form reports its single kernel as pass 1. */

@@ -318,8 +318,10 @@ void make_setup(Setup& S, int nprim, const double* alpha, const int* tmn, const 
 
 // Screening and set-up of one quartet (mod_intracule.f90:282-343). Returns a bitmask
 // (1 = passed screen 1, 2 = passed screen 2) and fills q when both pass.
+// Jtab (optional): JA8 of every primitive pair, Jtab[i * nprim + k], computed by ja8 with the
+// same arguments as here (so the same bits).
 int prepare_one(const Setup& S, int i, int j, int k, int l, double v, Quartet* q, double* s1out,
-                double* s2out) {
+                double* s2out, const double* Jtab = nullptr) {
   const Prim &Pi = S.prims[i], &Pj = S.prims[j], &Pk = S.prims[k], &Pl = S.prims[l];
   double DMval = v * (S.norm[i] * S.norm[j] * S.norm[k] * S.norm[l]);
   double aik = Pi.alpha + Pk.alpha, ajl = Pj.alpha + Pl.alpha;
@@ -329,8 +331,9 @@ int prepare_one(const Setup& S, int i, int j, int k, int l, double v, Quartet* q
     Rik2 += (Pi.x[d] - Pk.x[d]) * (Pi.x[d] - Pk.x[d]);
     Rjl2 += (Pj.x[d] - Pl.x[d]) * (Pj.x[d] - Pl.x[d]);
   }
-  double Jik = ja8(Pi, Pk, Rik2, aik, eik);
-  double Jjl = ja8(Pj, Pl, Rjl2, ajl, ejl);
+  const size_t np = S.prims.size();
+  double Jik = Jtab ? Jtab[i * np + k] : ja8(Pi, Pk, Rik2, aik, eik);
+  double Jjl = Jtab ? Jtab[j * np + l] : ja8(Pj, Pl, Rjl2, ajl, ejl);
   double screen1 = std::fabs(DMval) * std::sqrt(Jik * Jjl);
   if (s1out) *s1out = screen1;
   if (!(screen1 >= S.lim)) return 0;
@@ -736,6 +739,86 @@ int orc_intracule(int nprim, const double* alpha, const int* tmn, const double* 
     Ivec[g] = s;
   }
   if (counts) { counts[0] = nq; counts[1] = n1; counts[2] = n2; }
+  return 0;
+}
+
+// The hot path over a closed-shell DM2 generated from the 1-RDM D (nprim x nprim, column-major)
+// instead of read from a file: Gamma_{ik,jl} = D_ik D_jl - 1/2 D_il D_jk summed over the distinct
+// orderings (i,k)/(k,i) x (j,l)/(l,j), records (i,j,k,l) with i <= k and j <= l; unique != 0
+// keeps pair(ik) <= pair(jl) and doubles the off-diagonal pairs. The records are enumerated and
+// their values formed exactly as the library's device generator does (pairs in row-major packed
+// order), so screening sees the same values; they are evaluated in batches of 40960 as
+// orc_intracule does, without storing the list (the full lists of the larger synthetic workloads
+// do not fit in host memory as records).
+int orc_intracule_closed_shell(int nprim, const double* alpha, const int* tmn, const double* xyz, int normalize,
+                               double thresh, const double* D, int unique, long ngrid, const double* r,
+                               double* Ivec, long* counts, int nthreads) {
+  Setup S;
+  make_setup(S, nprim, alpha, tmn, xyz, normalize, thresh);
+  const long n = nprim;
+  std::vector<double> Jtab(n * n);
+  for (long i = 0; i < n; ++i)
+    for (long k = 0; k < n; ++k) {
+      const Prim &Pi = S.prims[i], &Pk = S.prims[k];
+      const double aik = Pi.alpha + Pk.alpha, eik = Pi.alpha * Pk.alpha * (1.0 / aik);
+      double Rik2 = 0;
+      for (int d = 0; d < 3; ++d) Rik2 += (Pi.x[d] - Pk.x[d]) * (Pi.x[d] - Pk.x[d]);
+      Jtab[i * n + k] = ja8(Pi, Pk, Rik2, aik, eik);
+    }
+  const long npair = n * (n + 1) / 2;
+  const long nrec = unique ? npair * (npair + 1) / 2 : npair * npair;
+  // packed pair p -> (a, b), a <= b, rows a = 0..m-1 of m - a entries
+  auto unpack = [](long p, long m, long* a, long* b) {
+    long lo = 0, hi = m - 1;
+    while (lo < hi) {
+      const long mid = (lo + hi + 1) / 2;
+      if (mid * m - mid * (mid - 1) / 2 <= p) lo = mid; else hi = mid - 1;
+    }
+    *a = lo;
+    *b = lo + (p - (lo * m - lo * (lo - 1) / 2));
+  };
+  auto gam = [&](long i, long k, long j, long l) {
+    return D[i + n * k] * D[j + n * l] - 0.5 * D[i + n * l] * D[j + n * k];
+  };
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  int nt = 1;
+#pragma omp parallel
+  {
+#pragma omp single
+    nt = omp_get_num_threads();
+  }
+  std::vector<std::vector<double>> priv(nt, std::vector<double>(ngrid, 0.0));
+  long n1 = 0, n2 = 0;
+  const long kBatch = 40960;
+  for (long b0 = 0; b0 < nrec; b0 += kBatch) {
+    const long b1 = std::min(nrec, b0 + kBatch);
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : n1, n2)
+    for (long rr = b0; rr < b1; ++rr) {
+      long pa, pb, i, k, j, l;
+      if (unique) unpack(rr, npair, &pa, &pb); else { pa = rr / npair; pb = rr % npair; }
+      unpack(pa, n, &i, &k);
+      unpack(pb, n, &j, &l);
+      const long ik[2][2] = {{i, k}, {k, i}}, jl[2][2] = {{j, l}, {l, j}};
+      const int nik = (i == k) ? 1 : 2, njl = (j == l) ? 1 : 2;
+      double v = 0.0;
+      for (int a = 0; a < nik; ++a)
+        for (int b = 0; b < njl; ++b) v += gam(ik[a][0], ik[a][1], jl[b][0], jl[b][1]);
+      if (unique && pa != pb) v *= 2.0;
+      Quartet Q;
+      const int f = prepare_one(S, int(i), int(j), int(k), int(l), v, &Q, nullptr, nullptr, Jtab.data());
+      if (f & 1) ++n1;
+      if (f & 2) {
+        ++n2;
+        accumulate(Q, ngrid, r, priv[omp_get_thread_num()].data());
+      }
+    }
+  }
+  for (long g = 0; g < ngrid; ++g) {
+    double s = 0.0;
+    for (int t = 0; t < nt; ++t) s += priv[t][g];
+    Ivec[g] = s;
+  }
+  if (counts) { counts[0] = nrec; counts[1] = n1; counts[2] = n2; }
   return 0;
 }
 

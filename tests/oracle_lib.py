@@ -49,6 +49,8 @@ def lib():
         L.orc_intracule.argtypes = [ctypes.c_int, DP, IP, DP, ctypes.c_int, ctypes.c_double, ctypes.c_long,
                                     IP, DP, ctypes.c_long, DP, DP, LP, ctypes.c_int]
         L.orc_eval_records.argtypes = [ctypes.c_long, DP, DP, DP, IP, DP, ctypes.c_long, DP, DP]
+        L.orc_intracule_closed_shell.argtypes = [ctypes.c_int, DP, IP, DP, ctypes.c_int, ctypes.c_double, DP,
+                                                 ctypes.c_int, ctypes.c_long, DP, DP, LP, ctypes.c_int]
         L.orc_radial_smearing.argtypes = [ctypes.c_long, DP, DP, DP, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_double, DP, DP, DP]
     return _lib
@@ -273,6 +275,21 @@ def intracule(sys_, thresh, r, normalize=True, nthreads=0):
     v = np.ascontiguousarray(sys_["v"], dtype=np.float64)
     lib().orc_intracule(len(alpha), _d(alpha), _i(tmn), _d(xyz), int(normalize), thresh, len(v), _i(ijkl), _d(v), ng,
                         _d(r), _d(Iv), counts.ctypes.data_as(LP), nthreads)
+    return Iv, counts
+
+
+def intracule_closed_shell(basis, D, thresh, r, unique=False, normalize=True, nthreads=0):
+    """The oracle over the closed-shell DM2 of the 1-RDM D, generated as the library's device
+    generator does (inca_gen_closed_shell_dm2), in batches; returns I at r and the counts."""
+    r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+    Iv = np.zeros(len(r))
+    counts = np.zeros(3, dtype=np.int64)
+    alpha = np.ascontiguousarray(basis["alpha"], dtype=np.float64)
+    tmn = np.ascontiguousarray(basis["tmn"], dtype=np.int32)
+    xyz = np.ascontiguousarray(basis["xyz"], dtype=np.float64)
+    Dc = np.ascontiguousarray(np.asarray(D, dtype=np.float64).T)  # column-major D(nprim, nprim)
+    lib().orc_intracule_closed_shell(len(alpha), _d(alpha), _i(tmn), _d(xyz), int(normalize), thresh, _d(Dc),
+                                     int(unique), len(r), _d(r), _d(Iv), counts.ctypes.data_as(LP), nthreads)
     return Iv, counts
 
 

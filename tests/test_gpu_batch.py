@@ -1,12 +1,16 @@
 """Batches of molecules (inca_batch_*): I(s) of every molecule from one batched evaluation
-against the same molecules evaluated one at a time.
+against the same molecules evaluated one at a time, and against the CPU oracle.
 
-Tolerances: FP64 form 1e-12 relative per I(s) (only the split of the quartet sums differs);
-mixed form 1e-8 relative per I(s) against the per-molecule FP64 form; quartet counts equal to
-the sums of the per-molecule counts.
+Tolerances: FP64 form 1e-12 relative per I(s) against single runs (only the split of the
+quartet sums differs); mixed form 1e-8 relative per I(s) against the per-molecule FP64 form;
+quartet counts equal to the sums of the per-molecule counts. Against the oracle (molecules with
+d shells, exponents up to 200): counts identical per molecule, FP64 I(s) within 1e-11 relative
+(+ 1e-13 of the molecule's max|I(s)|), mixed within 1e-8 relative (+ 1e-12 of max|I(s)|).
 """
 import numpy as np
 import pytest
+
+import oracle_lib as O
 
 pytestmark = pytest.mark.gpu
 
@@ -98,3 +102,37 @@ def test_waves_match_one_batch(ctx, molecules):
     for a, m, r in zip(I64, Im, ref64):
         np.testing.assert_allclose(a, r, rtol=1e-12, atol=0)
         assert np.max(np.abs(m - r) / np.abs(r)) <= 1e-8
+
+
+@pytest.fixture(scope="module")
+def molecules_d():
+    from inca_parallel_gb300 import workloads as W
+    rng = np.random.default_rng(W.SEED0 + 33)
+    mols = []
+    for natoms, nprim in [(3, 30), (4, 40), (5, 45), (6, 36)]:
+        b = W.random_molecule(rng, natoms, nprim, hi=200.0)
+        nocc = max(1, min(W.electrons(b) // 2, len(b["alpha"]) // 3))
+        D, _ = W.closed_shell_density(b, nocc, int(rng.integers(1 << 30)))
+        mols.append((b, D))
+    assert any(int(b["tmn"].sum(1).max()) == 2 for b, _ in mols)
+    return mols
+
+
+def test_batch_with_d_shells_matches_oracle(ctx, molecules_d):
+    g = O.gridpoints2(*SCAN)
+    seg = np.repeat(np.arange(len(g["smn"])), g["smn"])
+    ctx.batch_clear()
+    for b, D in molecules_d:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN)
+    counts = ctx.batch_prepare(THRESH)
+    I64 = ctx.batch_eval(mode=0)
+    Imx = ctx.batch_eval(mode=1, tol=1e-8)
+    tot = np.zeros(3, dtype=np.int64)
+    for (b, D), a, m in zip(molecules_d, I64, Imx):
+        Io, oc = O.intracule_closed_shell(b, D, THRESH, g["r"])
+        tot += oc
+        ref = np.bincount(seg, weights=g["w_ang"] * Io, minlength=len(g["smn"]))
+        scale = np.abs(ref).max()
+        np.testing.assert_allclose(a, ref, rtol=1e-11, atol=1e-13 * scale)
+        assert np.all(np.abs(m - ref) <= 1e-8 * np.abs(ref) + 1e-12 * scale)
+    assert list(counts) == tot.tolist()

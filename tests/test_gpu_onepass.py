@@ -77,6 +77,25 @@ def test_estimate_pass_items(ctx, scan_fp64, monkeypatch, items):
     np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
 
 
+@pytest.mark.parametrize("cheap,drop", [("1", "0.4"), ("1", "0.05"), ("0", "0.05")])
+def test_cheap_tier(ctx, scan_fp64, monkeypatch, cheap, drop):
+    # pairs whose rigorous FP32 error bound fits under the drop threshold take the cheap tier
+    # (plain FP32, hardware ex2); the tolerance holds with and without it, and with a large
+    # share of the tolerance given to left-out and cheap pairs
+    monkeypatch.setenv("INCA_CHEAP_TIER", cheap)
+    monkeypatch.setenv("INCA_DROP_FRACTION", drop)
+    I = _scan_mixed(ctx)
+    rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+    assert rel.max() <= 1e-8, rel.max()
+    st = ctx.stats()
+    if cheap == "1":
+        assert st["cheap_pairs"] > 0
+    else:
+        assert st["cheap_pairs"] == 0
+    eager = ctx.eval(mode=1, tol=1e-8)
+    np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+
+
 def test_one_pass_deterministic(ctx):
     a = _scan_mixed(ctx)
     b = _scan_mixed(ctx)
