@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-ring", dest="ring", action="store_false",
+                   help="leave out the 12-atom ring's radial-integral leg (about 45 s)")
     return p.parse_args()
 
 
@@ -173,6 +175,56 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ 12-atom ring leg
+def ring_leg(ctx, stream, flush):
+    """Radial integral of the 12-atom ring (198 primitives, l <= 2, exponents 0.1-5000, 21
+    occupied orbitals, symmetry-unique DM2 of 194 074 551 records generated on the device),
+    nrad 75, nang 302 on the automatic centres (nosym), thresh 1e-12: the mixed form at 1e-10
+    on the whole grid, and the plain FP64 form on every 97th grid point, whose rate gives the
+    FP64 time of the whole grid. Error: the mixed form's values at those points against the FP64
+    form's, relative to the largest |I| there."""
+    import torch
+    from inca_parallel_gb300 import INCA_FP64, INCA_MIXED, centercalc, workloads as W
+    b, D = W.ring_workload()
+    ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+    nrec = ctx.gen_closed_shell_dm2(D, unique=True)
+    counts = ctx.prepare(THRESH)
+    cent, Ps, alf = centercalc(b["an"], b["cartes"])
+    ctx.grid_radial([75] * len(Ps), [302] * len(Ps), alf, cent, Ps, nosym=True)
+    ng = ctx.ngrid
+    pts = ctx.grid_copy(weights=False)["r"]
+
+    def run(fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), out
+
+    def mixed():
+        I = ctx.eval(mode=INCA_MIXED, tol=TOL_INTEGRAL)
+        return I, ctx.radial_integral()[0]
+
+    run(mixed)  # sorts the grid and sizes the buffers
+    t_mix, (Imix, R) = run(mixed)
+    stats = ctx.stats()
+    sub = np.arange(0, ng, 97)
+    ctx.grid_points(pts[sub])
+    t_sub, I64 = run(lambda: ctx.eval(mode=INCA_FP64))
+    rate64 = counts[2] * len(sub) / (t_sub * 1e-3)
+    qp = counts[2] * ng
+    err = float(np.abs(Imix[sub] - I64).max() / np.abs(I64).max())
+    return {"records": int(nrec), "survivors": int(counts[2]), "grid_points": int(ng), "centres": int(len(Ps)),
+            "tolerance": TOL_INTEGRAL, "radial_integral": R, "mixed_ms": t_mix,
+            "mixed_value": qp / (t_mix * 1e-3), "fp64_value_sampled": rate64,
+            "fp64_ms_whole_grid_at_sampled_rate": qp / rate64 * 1e3, "fp64_sample_points": int(len(sub)),
+            "speedup_vs_fp64_form": qp / rate64 * 1e3 / t_mix, "max_err_rel_max_at_sample": err,
+            "tiers": stats}
+
+
 # ------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import torch
@@ -181,7 +233,7 @@ def gpu_arm(args):
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from inca_parallel_gb300 import INCA_FP64, INCA_MIXED, Context
+    from inca_parallel_gb300 import INCA_FP64, INCA_FP64_SCREENED, INCA_MIXED, Context
     b, D, ijkl, v = workload()
     ctx = Context(local)
     ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
@@ -236,10 +288,16 @@ def gpu_arm(args):
     with ClockSampler(local) as clk:
         tm, km, wall, Imix, launches = timed(INCA_MIXED, TOL_SCAN, args.steps, args.warmup)
     stats = ctx.stats()
+    # the FP64 form with the same leaving-out of negligible (quartet, tile) pairs, on the same
+    # schedule: the mixed form against it differs only in the arithmetic of the terms
+    t64s, _, _, I64s, _ = timed(INCA_FP64_SCREENED, TOL_SCAN, max(2, args.steps // 3), 1)
+    stats64s = ctx.stats()
     ctx.set_tuning()  # the radial-integral and cube legs run the default schedule
     ms = statistics.mean(tm)
     ms64 = statistics.mean(t64)
+    ms64s = statistics.mean(t64s)
     rel_scan = float(np.max(np.abs(Imix - I64) / np.abs(I64)))
+    rel_scan64s = float(np.max(np.abs(I64s - I64) / np.abs(I64)))
     # radial integral (nrad 50, nang 110, multicentre centres of CH4): time and error, both forms
     from inca_parallel_gb300 import centercalc
     cent, Ps, alf = centercalc(b["an"], b["cartes"])
@@ -281,6 +339,8 @@ def gpu_arm(args):
         cube[name] = {"ms": statistics.mean(ts), "I": ctx.eval(mode=mode, tol=TOL_CUBE)}
     cube_err = float(np.abs(cube["mixed"]["I"] - cube["fp64"]["I"]).max() / np.abs(cube["fp64"]["I"]).max())
     cube_qp = counts[2] * int(np.prod(CUBE[2]))
+
+    ring = ring_leg(ctx, stream, flush) if args.ring else None
 
     # end to end through the C ABI with host buffers (the call sequence of the Fortran program's
     # bind(C) shim), tuned schedule;
@@ -371,6 +431,14 @@ def gpu_arm(args):
                        "radial_integral_nrad50_nang110": {"fp64_ms": ri["fp64"]["ms"], "mixed_ms": ri["mixed"]["ms"],
                                                           "rel_err": ri_rel, "value": ri["fp64"]["value"],
                                                           "tolerance": TOL_INTEGRAL},
+                       "fp64_screened_form": {"ms_per_step": ms64s, "value": qp / (ms64s * 1e-3),
+                                              "max_rel_err_I_s_vs_fp64": rel_scan64s,
+                                              "pairs_evaluated": stats64s["precise_pairs"],
+                                              "pairs_left_out": stats64s["skipped_pairs"],
+                                              "note": "every term in FP64, leaving out the same negligible "
+                                                      "(quartet, tile) pairs as the mixed form, same schedule"},
+                       "speedup_vs_fp64_screened_form": ms64s / ms,
+                       "ring_radial_integral": ring,
                        "vector_cube_48": {"fp64_ms": cube["fp64"]["ms"], "mixed_ms": cube["mixed"]["ms"],
                                           "mixed_value": cube_qp / (cube["mixed"]["ms"] * 1e-3),
                                           "max_err_rel_max": cube_err, "tolerance": TOL_CUBE,

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libinca_gpu.so")
 INCA_OK = 0
 INCA_FP64 = 0
 INCA_MIXED = 1
+INCA_FP64_SCREENED = 2
 MAX_COEF = 17
 STATUS = {0: "INCA_OK", 1: "INCA_E_ARG", 2: "INCA_E_CUDA", 3: "INCA_E_IO", 4: "INCA_E_FORMAT",
           5: "INCA_E_STATE", 6: "INCA_E_NOMEM", 7: "INCA_E_LIMIT", 8: "INCA_E_TIMEOUT"}

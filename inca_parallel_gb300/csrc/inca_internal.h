@@ -262,6 +262,7 @@ int ensure_exp_table(inca_ctx* c);
 // cube_eval.cu
 bool cube_separable(const inca_ctx* c);
 int eval_cube_separable(inca_ctx* c, double eps);
+int eval_fp64_screened(inca_ctx* c, double eps, bool* plain);
 
 // grid_build.cu
 int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nangc,

@@ -113,7 +113,17 @@ int eval_device(inca_ctx* c, int mode, double tol, bool graph) {
     if (st == INCA_OK) c->evaluated = true;
     return st;
   }
-  if (mode != INCA_FP64) return set_error(c, INCA_E_ARG, "inca_eval: unknown mode");
+  if (mode == INCA_FP64_SCREENED && !cube_separable(c)) {
+    bool plain = false;
+    const int st = eval_fp64_screened(c, tol > 0 ? tol : 1e-10, &plain);
+    if (st != INCA_OK) return st;
+    if (!plain) {
+      c->evaluated = true;
+      return INCA_OK;
+    }
+  } else if (mode != INCA_FP64 && mode != INCA_FP64_SCREENED) {
+    return set_error(c, INCA_E_ARG, "inca_eval: unknown mode");
+  }
   const int64_t ngrid = c->ngrid;
   const int nchunks = static_cast<int>(c->chunks.size());
   cudaEvent_t e0, e1, e2;

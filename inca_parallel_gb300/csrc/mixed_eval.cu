@@ -756,6 +756,149 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
   }
 }
 
+// ---------------------------------------------------------------- FP64 form, screened
+// The plain FP64 form with the one-pass form's leaving-out of negligible (quartet, tile) pairs:
+// the same persistent work items, staging, tile bounds and drop thresholds as k_pass1<true>, and
+// every remaining term in FP64 (the hi + lo pairs of the FP32 records carry each value to about
+// 2^-48), without error bounds or corrections. It prices the precision alone: the mixed form
+// against this kernel differs only in the arithmetic of the terms it evaluates.
+__device__ __forceinline__ void term_f64(const float* __restrict__ R, const int L[3], const double (&x)[3][kPPT],
+                                         double (&acc)[kPPT]) {
+  const double s = static_cast<double>(R[0]) + static_cast<double>(R[1]);
+  const double b[3] = {static_cast<double>(R[2]) + static_cast<double>(R[5]),
+                       static_cast<double>(R[3]) + static_cast<double>(R[6]),
+                       static_cast<double>(R[4]) + static_cast<double>(R[7])};
+  const double m = static_cast<double>(R[8]) + static_cast<double>(R[9]);
+  const double ks = static_cast<double>(R[11]);
+  const int nc = L[0] + L[1] + L[2] + 3;
+  double u[3][kPPT], t[kPPT];
+#pragma unroll
+  for (int p = 0; p < kPPT; ++p) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d][p] = fma(s, x[d][p], b[d]);
+    const double y = -(u[0][p] * u[0][p] + u[1][p] * u[1][p] + u[2][p] * u[2][p]);
+    t[p] = m * exp2(y + ks);
+  }
+  int o = 12;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (L[d]) {
+      double v[kPPT];
+      const double c0 = static_cast<double>(R[o]) + static_cast<double>(R[o + nc]);
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) v[p] = c0;
+#pragma unroll 1
+      for (int k = 1; k <= L[d]; ++k) {
+        const double ck = static_cast<double>(R[o + k]) + static_cast<double>(R[o + k + nc]);
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) v[p] = fma(v[p], u[d][p], ck);
+      }
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) t[p] *= v[p];
+    }
+    o += L[d] + 1;
+  }
+#pragma unroll
+  for (int p = 0; p < kPPT; ++p) acc[p] += t[p];
+}
+
+__global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
+k_pass_f64(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
+           const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
+           const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
+           int64_t nitems, int stage_floats, const float* __restrict__ lt_drop, double* __restrict__ part,
+           double* __restrict__ part_abs, double* __restrict__ drop_mass, unsigned long long* __restrict__ work,
+           unsigned long long* __restrict__ stats, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char dsm[];
+  const Stage S = stage_view(dsm, stage_floats);
+  const int lane = threadIdx.x;
+  stage_init(S);
+  unsigned long long nskip = 0, nlive = 0;
+  int k = 0;
+  for (;;) {
+    const int64_t item = next_item(work);
+    if (item >= nitems) break;
+    int64_t wtile, pat, dat;
+    int nsplit, first;
+    ChunkRange cr;
+    {
+      const MolWork& W = mw[mol_of_item(mw, nmol, item)];
+      const int64_t local = item - W.item0;
+      const int64_t tl = local / W.nsplit;
+      const int split = static_cast<int>(local - tl * W.nsplit);
+      nsplit = W.nsplit;
+      wtile = W.tile0 + tl;
+      cr = ChunkRange{W.cb, W.ce};
+      first = cr.begin + split;
+      pat = W.poff + static_cast<int64_t>(split) * W.np - W.p0;
+      dat = W.doff + static_cast<int64_t>(split) * W.ntiles + tl;
+    }
+    const TileInfo T = tiles[wtile];
+    if (first < cr.end) stage_first(S, chunks, segs, rec32, k, first);
+    double x[3][kPPT], acc[kPPT];
+    {
+      float rh[3][kPPT], rl[3][kPPT];
+      load_points(phi, plo, T, lane, rh, rl);
+#pragma unroll
+      for (int p = 0; p < kPPT; ++p) {
+        acc[p] = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d][p] = static_cast<double>(rh[d][p]) + static_cast<double>(rl[d][p]);
+      }
+    }
+    float box[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) box[b] = wtbox[wtile * 8 + b];
+    const float thr = lt_drop ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
+    float dm = 0.0f;
+    __syncwarp();
+    bool ok = true;
+    for (int ch = first; ch < cr.end; ch += nsplit, ++k) {
+      ok = __all_sync(0xffffffffu, stage_next(S, chunks, segs, rec32, k, ch + nsplit, cr.end));
+      if (!ok) break;
+      const WorkChunk w = chunks[ch];
+      const ClassSeg sg = segs[w.cls];
+      const float* st = S.buf(k);
+      const int L[3] = {__reduce_max_sync(0xffffffffu, sg.L[0]), __reduce_max_sync(0xffffffffu, sg.L[1]),
+                        __reduce_max_sync(0xffffffffu, sg.L[2])};
+      const int rs = __reduce_max_sync(0xffffffffu, sg.stride32);
+      const float lb = lane < w.count ? log2_bound(st + lane * rs, L, box) : -HUGE_VALF;
+      uint32_t m = __ballot_sync(0xffffffffu, lane < w.count && lb > thr);
+      if (lane < w.count && !(lb > thr)) dm += exp2f(lb);
+      if (lane == 0) {
+        nskip += w.count - __popc(m);
+        nlive += __popc(m);
+      }
+      while (m) {
+        const int q = __ffs(m) - 1;
+        m &= m - 1;
+        term_f64(st + q * rs, L, x, acc);
+      }
+      __syncwarp();
+    }
+    if (!ok) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) {
+      const int j = lane + 32 * p;
+      if (j < T.count) {
+        part[pat + T.start + j] = acc[p];
+        part_abs[pat + T.start + j] = 0.0;
+      }
+    }
+    if (drop_mass) {
+      for (int o = 16; o > 0; o >>= 1) dm += __shfl_xor_sync(0xffffffffu, dm, o);
+      if (lane == 0) drop_mass[dat] = dm * 1.0001;
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(&stats[0], nlive);
+    atomicAdd(&stats[2], nskip);
+  }
+}
+
 // ---------------------------------------------------------------- pass 2 (corrections)
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
@@ -1439,6 +1582,7 @@ double env_knob(const char* name, double dflt, double lo, double hi) {
 struct MixedPlan {
   bool fused = false;
   int mode = 2, nseg = 1, emode = 0, nmol = 1, cheap = 1, wait_test = 0;
+  bool f64 = false;  // the screened FP64 form (k_pass_f64 instead of the FP32 passes)
   const int* seg_of = nullptr;
   int64_t ngrid = 0, nwt = 0, ngroups = 0, nitems = 0, npart = 0, ndrop = 0;
   int64_t ns = 0, nitems_s = 0, npart_s = 0;
@@ -1633,7 +1777,11 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
   // terms below the drop thresholds left out)
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[1], c->stream));
-  if (P.fused)
+  if (P.f64)
+    INCA_LAUNCH(c, k_pass_f64, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+                c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, use_drop ? P.ltdrop : nullptr, P.p1,
+                P.pabs, use_drop ? P.dmass : nullptr, P.work, P.stats, P.errw);
+  else if (P.fused)
     INCA_LAUNCH(c, k_pass1<true>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,
                 use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw, P.wait_test);
@@ -1675,12 +1823,15 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   // every item whose tile has none)
   if (P.fused) INCA_LAUNCH(c, k_band, P.gblk, 256, 0, tiles, P.ngroups, P.ptau, P.ptau_est, P.glt, P.stats + 12);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[3], c->stream));
-  INCA_LAUNCH(c, k_pass2, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
-              c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
-              use_drop ? P.ltdrop : nullptr, P.cheap, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1, P.stats + 4,
-              P.errw);
+  if (!P.f64) {  // the screened FP64 form has nothing to correct
+    INCA_LAUNCH(c, k_pass2, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+                c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
+                use_drop ? P.ltdrop : nullptr, P.cheap, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1,
+                P.stats + 4, P.errw);
+  }
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[4], c->stream));
-  INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, P.p2, P.Is);
+  INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, P.f64 ? nullptr : P.p2,
+              P.Is);
   INCA_LAUNCH(c, k_scatter, nblk(ngrid), 256, 0, ngrid, c->d_perm.p, P.Is, c->d_ivec.p);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[5], c->stream));
   INCA_CUDA(c, cudaGetLastError());
@@ -1757,6 +1908,42 @@ int eval_mixed(inca_ctx* c, double eps) {
     if ((st = mixed_launch(c, P, false, &ev))) return st;
     if ((st = mixed_finish(c, P, &ev, &retry))) return st;
   }
+  c->t_launches = static_cast<int>(c->launches - launches0);
+  return INCA_OK;
+}
+
+// The screened FP64 form: the one-pass form's plan (estimate pass, drop thresholds, left-out mass
+// check and repetition without leaving out) with k_pass_f64 as the pass over all terms. Grids
+// below the one-pass size, and cube lattices, have no drop thresholds: there it is the FP64 form.
+int eval_fp64_screened(inca_ctx* c, double eps, bool* plain) {
+  *plain = false;
+  if (c->chunks.empty()) {
+    INCA_CUDA(c, cudaMemsetAsync(c->d_ivec.p, 0, sizeof(double) * c->ngrid, c->stream));
+    INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return INCA_OK;
+  }
+  const int64_t launches0 = c->launches;
+  MixedPlan P;
+  int st = mixed_plan(c, eps, P);
+  if (st) return st;
+  if (!P.fused || P.drop_frac <= 0.0) {
+    *plain = true;
+    return INCA_OK;
+  }
+  P.f64 = true;
+  P.cheap = 0;
+  Events ev;
+  for (auto& e : ev.e) INCA_CUDA(c, cudaEventCreate(&e));
+  bool retry = false;
+  if ((st = mixed_launch(c, P, true, &ev))) return st;
+  if ((st = mixed_finish(c, P, &ev, &retry))) return st;
+  if (retry) {
+    if ((st = mixed_launch(c, P, false, &ev))) return st;
+    if ((st = mixed_finish(c, P, &ev, &retry))) return st;
+  }
+  c->pairs_fp64 = c->pairs_fp32;  // the pairs evaluated (in FP64 here)
+  c->pairs_fp32 = 0;
+  c->corrected_points = 0;
   c->t_launches = static_cast<int>(c->launches - launches0);
   return INCA_OK;
 }

@@ -43,6 +43,11 @@ extern "C" {
 #define INCA_FP64 0  /* every quartet-point term in FP64 (the plain GPU form)              */
 #define INCA_MIXED 1 /* FP32 terms with FP64 accumulation; terms whose FP32 error could
                         exceed the requested tolerance are evaluated in FP64             */
+#define INCA_FP64_SCREENED 2 /* every term in FP64, leaving out the negligible (quartet,
+                        tile) pairs that INCA_MIXED leaves out, within the same share of the
+                        tolerance (grids of 2 048 points or more; cube lattices and smaller
+                        grids run as INCA_FP64). No counterpart in the reference: it prices
+                        the precision alone against INCA_MIXED                           */
 
 /* maximum per-dimension polynomial degree t_i+t_j+t_k+t_l (g shells: 16) */
 #define INCA_MAX_DEGREE 16
@@ -138,8 +143,8 @@ int inca_grid_copy(inca_ctx* ctx, double* r, double* w, double* wvee, int32_t* c
 /* ---- evaluation and reductions ---- */
 
 /* Evaluate I at every point of the resident grid (mod_intracule.f90:345-358, all quartets).
- * mode: INCA_FP64 or INCA_MIXED; tol: relative tolerance of the mixed form on the grid's
- * outputs (ignored for INCA_FP64; <= 0 selects 1e-10). ivec (ngrid) may be NULL (result
+ * mode: INCA_FP64, INCA_MIXED or INCA_FP64_SCREENED; tol: relative tolerance of the mixed form
+ * on the grid's outputs (ignored for INCA_FP64; <= 0 selects 1e-10). ivec (ngrid) may be NULL (result
  * stays on the device for the reductions). On a cube lattice (inca_grid_cube, one molecule)
  * INCA_MIXED evaluates the lattice's separable factors in double-float (about 2^-44 relative
  * per term) and leaves out only quartets whose terms sum to at most 5% of tol times max|I|;

@@ -96,6 +96,22 @@ def test_cheap_tier(ctx, scan_fp64, monkeypatch, cheap, drop):
     np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
 
 
+def test_fp64_screened_form(ctx, scan_fp64):
+    # every term in FP64 with the mixed form's leaving-out of negligible (quartet, tile) pairs:
+    # the left-out bound mass is checked after the pass to stay within half the tolerance (else
+    # the pass is repeated without leaving out), so the result is within 0.5e-8 of the plain form
+    from inca_parallel_gb300 import INCA_FP64_SCREENED
+    ctx.grid_scan(*SCAN)
+    ctx.eval(mode=INCA_FP64_SCREENED, tol=1e-8)
+    I = ctx.radial_plot()[1]
+    rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
+    assert rel.max() <= 0.5e-8, rel.max()
+    st = ctx.stats()
+    assert st["skipped_pairs"] > 0 and st["precise_pairs"] > 0 and st["corrected_terms"] == 0
+    np.testing.assert_array_equal(ctx.eval(mode=INCA_FP64_SCREENED, tol=1e-8), ctx.eval(mode=INCA_FP64_SCREENED,
+                                                                                      tol=1e-8))
+
+
 def test_one_pass_deterministic(ctx):
     a = _scan_mixed(ctx)
     b = _scan_mixed(ctx)
