@@ -47,6 +47,11 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-ring", dest="ring", action="store_false",
                    help="leave out the 12-atom ring's radial-integral leg (about 45 s)")
+    p.add_argument("--no-batch", dest="batch", action="store_false",
+                   help="leave out the batched-molecules leg")
+    p.add_argument("--shard", default="replicas", choices=["replicas", "points"],
+                   help="N > 1: each rank evaluates its own copy of the workload (replicas, weak scaling) or "
+                        "its share of the scan's shells (points, strong scaling: one scan split over the ranks)")
     return p.parse_args()
 
 
@@ -175,6 +180,17 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def scan_for_rank(shard, rank, world):
+    """grid_scan arguments of this rank: the whole scan, or its share of the shells."""
+    if not shard or world == 1:
+        return SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"]
+    from inca_parallel_gb300 import sharding as SH
+    part = SH.scan_shard(SCAN["start"][0], SCAN["end"][0], SCAN["step"][0], rank, world)
+    if part is None:
+        raise SystemExit("more ranks than shells")
+    return [part[0]], [part[1]], SCAN["step"], SCAN["nang"]
+
+
 # ------------------------------------------------------------------ 12-atom ring leg
 def ring_leg(ctx, stream, flush):
     """Radial integral of the 12-atom ring (198 primitives, l <= 2, exponents 0.1-5000, 21
@@ -225,6 +241,69 @@ def ring_leg(ctx, stream, flush):
             "tiers": stats}
 
 
+# ------------------------------------------------------------------ batched molecules leg
+def batch_leg(ctx, device):
+    """Molecules of the 64-molecule batch workload (3-20 atoms, 20-300 primitives, exponents up
+    to 200, symmetry-unique closed-shell DM2s) with at most 60 primitives -- a subset that fits
+    one batch -- each as radial_plot s = 0..10 step 0.1 at nang 302 (nosym), thresh 1e-12, with
+    records and grids resident: one batched preparation plus one replay of the captured
+    evaluation graph (mixed, 1e-8 per I(s)) and the I(s) reduction, against the molecules run one
+    after the other (preparation, plain FP64 evaluation, I(s)), each in its own context. Host
+    wall time around the (synchronous) calls."""
+    from inca_parallel_gb300 import INCA_FP64, INCA_MIXED, Context, workloads as W
+    scan = ([0.0], [10.0], [0.1], [302])
+    mols = W.batch_workload(max_prims=60)
+    ctxs = []
+    for _, b, D in mols:
+        c = Context(device)
+        c.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+        c.gen_closed_shell_dm2(D, unique=True)
+        c.grid_scan(*scan, nosym=True)
+        ctxs.append(c)
+    ctx.batch_clear()
+    for _, b, D in mols:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *scan, unique=True, nosym=True)
+    cnt = ctx.batch_prepare(THRESH)
+
+    def batched():
+        ctx.prepare(THRESH)
+        ctx.eval_graph(mode=INCA_MIXED, tol=TOL_SCAN, copy=False)
+        return ctx.radial_plot()[1]
+
+    def sequential(mode):
+        res, qp = [], 0
+        for c in ctxs:
+            n = c.prepare(THRESH)
+            c.eval(mode=mode, tol=TOL_SCAN, copy=False)
+            res.append(c.radial_plot()[1])
+            qp += n[2] * c.ngrid
+        return np.concatenate(res), qp
+
+    def wall(fn, reps):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts) * 1e3, out
+
+    t_b, Ib = wall(batched, 5)  # the first call captures the graph; the timed ones replay it
+    t_64, (I64, qp) = wall(lambda: sequential(INCA_FP64), 2)
+    t_mx, _ = wall(lambda: sequential(INCA_MIXED), 3)
+    for c in ctxs:
+        c.close()
+    err = float(np.max(np.abs(Ib - I64) / np.abs(I64)))
+    return {"molecules": len(mols), "of_workload": 64, "primitives": [len(b["alpha"]) for _, b, _ in mols],
+            "records": int(cnt[0]), "survivors": int(cnt[2]), "grid_points": int(ctx.ngrid),
+            "quartet_points": int(qp), "batched_graph_ms": t_b, "batched_value": qp / (t_b * 1e-3),
+            "sequential_fp64_ms": t_64, "sequential_mixed_ms": t_mx,
+            "speedup_vs_sequential_fp64": t_64 / t_b, "speedup_vs_sequential_mixed": t_mx / t_b,
+            "max_rel_err_I_s_vs_fp64": err, "tolerance_I_s": TOL_SCAN,
+            "note": "batched: one preparation of the whole batch and one graph replay of its mixed "
+                    "evaluation; sequential: one context per molecule; preparation and I(s) on both sides"}
+
+
 # ------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import torch
@@ -239,7 +318,9 @@ def gpu_arm(args):
     ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
     ctx.set_quartets(ijkl, v)
     counts = ctx.prepare(THRESH)
-    nradi, ngrid = ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+    shard = args.shard == "points"
+    scan_args = scan_for_rank(shard, rank, world)
+    nradi, ngrid = ctx.grid_scan(*scan_args)
     rec = ctx.records()
     Lbar = float(rec["L"].sum(axis=1).mean())
     qp = counts[2] * ngrid
@@ -341,12 +422,13 @@ def gpu_arm(args):
     cube_qp = counts[2] * int(np.prod(CUBE[2]))
 
     ring = ring_leg(ctx, stream, flush) if args.ring else None
+    batch = batch_leg(ctx, local) if args.batch else None
 
     # end to end through the C ABI with host buffers (the call sequence of the Fortran program's
     # bind(C) shim), tuned schedule;
     # the quartet input and the I(r) output live in pinned host memory
     ctx.set_tuning(sched["items_per_cta"], sched["sample_stride"], sched["estimate_safety"], sched["drop_fraction"])
-    ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+    ctx.grid_scan(*scan_args)
     pin_ijkl = torch.empty(ijkl.size, dtype=torch.int32, pin_memory=True).numpy()
     pin_v = torch.empty(v.size, dtype=torch.float64, pin_memory=True).numpy()
     pin_out = torch.empty(ngrid, dtype=torch.float64, pin_memory=True).numpy()
@@ -362,7 +444,7 @@ def gpu_arm(args):
         ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
         ctx.set_quartets(pin_ijkl, pin_v)
         ctx.prepare(THRESH)
-        ctx.grid_scan(SCAN["start"], SCAN["end"], SCAN["step"], SCAN["nang"])
+        ctx.grid_scan(*scan_args)
         ctx.eval(mode=INCA_MIXED, tol=TOL_SCAN, out=pin_out)
         ctx.radial_plot()
         torch.cuda.synchronize()
@@ -388,11 +470,19 @@ def gpu_arm(args):
 
     # whole-job aggregate: max time over ranks (each rank evaluates its own copy: weak scaling)
     t_step = ms
+    qp_all, e2e_all = world * qp, world * qp / e2e_s
+    if world > 1 and shard:  # strong scaling: the ranks' shares add up to one scan
+        tq = torch.tensor([float(qp)], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(tq)
+        qp_all = float(tq.item())
+        te = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+        e2e_all = qp_all / float(te.item())
     if world > 1:
         tt = torch.tensor([t_step], device=f"cuda:{local}")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_step = float(tt.item())
-    value = world * qp / (t_step * 1e-3)
+    value = qp_all / (t_step * 1e-3)
     if rank == 0:
         prof = os.path.join(ROOT, "profiles", "k_pass1_ch4_radial_scan_590.md")
         traffic = None
@@ -413,10 +503,13 @@ def gpu_arm(args):
         hbm_gbs = traffic / (kms * 1e-3) / 1e9 if traffic else None
         line = {
             "metric": METRIC, "value": value, "unit": "quartet-points/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
+            "scaling": "strong" if (shard and world > 1) else "weak",
             "vs_baseline": None, "dtype": "f32 (double-float correction tier, f64 accumulation)",
             "data": "synthetic (seeded CH4 closed-shell DM2, 5 orbitals)",
             "config": {"workload": "ch4_radial_scan_590", "system": "CH4 27 primitives", "quartets": int(counts[0]),
+                       "parallelism": (f"points split over {world} ranks (whole shells)" if (shard and world > 1)
+                                       else f"{world} replica(s), one per GPU"),
                        "survivors": int(counts[2]), "grid_points": int(ngrid), "shells": int(nradi), "nang": 590,
                        "thresh": THRESH, "tolerance_I_s": TOL_SCAN, "l2": "flushed before each step (256 MiB write)",
                        "mean_L": Lbar,
@@ -439,6 +532,7 @@ def gpu_arm(args):
                                                       "(quartet, tile) pairs as the mixed form, same schedule"},
                        "speedup_vs_fp64_screened_form": ms64s / ms,
                        "ring_radial_integral": ring,
+                       "batched_graph": batch,
                        "vector_cube_48": {"fp64_ms": cube["fp64"]["ms"], "mixed_ms": cube["mixed"]["ms"],
                                           "mixed_value": cube_qp / (cube["mixed"]["ms"] * 1e-3),
                                           "max_err_rel_max": cube_err, "tolerance": TOL_CUBE,
@@ -456,7 +550,7 @@ def gpu_arm(args):
                          "tensor_view": {"achieved": 0.0, "unit": "TFLOP/s",
                                          "note": "sm__pipe_tensor_cycles_active 0 % (ncu)"}},
             "clocks": csum,
-            "e2e": {"value": qp / e2e_s, "unit": "quartet-points/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": e2e_all, "unit": "quartet-points/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
             "gpu_launches": int(launches),
         }

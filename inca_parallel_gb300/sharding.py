@@ -125,6 +125,44 @@ def sharded_radial_plot(evaluate, points, w_ang, smn, group=None):
     return sum_in_rank_order(local, group)
 
 
+def scan_shard(start, end, step, rank, world):
+    """The rank's share of one radial-scan block (shells s_k = start + k step, k < npb, as
+    gridpoints2 counts them: npb = int((end - start) / step) + 1): a contiguous run of whole
+    shells, itself a scan block (start', end', step) -- so each rank builds its part of the grid
+    on its own device and every I(s) is summed on one rank. Returns (start', end', k0, k1), or
+    None for a rank with no shell."""
+    if world < 1 or not 0 <= rank < world or not step > 0:
+        raise ValueError("bad shard arguments")
+    npb = int((end - start) / step) + 1
+    k0, k1 = (npb * rank) // world, (npb * (rank + 1)) // world
+    if k1 <= k0:
+        return None
+    s0 = start + k0 * step
+    # half a step past the last shell, so the shell count comes out exact despite rounding
+    return s0, s0 + (k1 - k0 - 1 + 0.5) * step, k0, k1
+
+
+def sharded_scan_plot(ctx, start, end, step, nang, mode, tol=1e-8, nosym=False, group=None):
+    """I(s) of one radial-scan block with its shells split over ranks: each rank builds and
+    evaluates its own shells (mixed form: the one-pass scan evaluation with its per-shell
+    tolerance), then the shells are gathered in order. ctx: a prepared Context on this rank's
+    GPU. Returns the full I(s) array (every rank)."""
+    dist = _dist()
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    npb = int((end - start) / step) + 1
+    local = np.zeros(npb)
+    part = scan_shard(start, end, step, rank, world)
+    if part is not None:
+        s0, s1, k0, k1 = part
+        nr, _ = ctx.grid_scan([s0], [s1], [step], [nang], nosym=nosym)
+        if nr != k1 - k0:
+            raise RuntimeError("scan shard: shell count mismatch")
+        ctx.eval(mode=mode, tol=tol, copy=False)
+        local[k0:k1] = ctx.radial_plot()[1]
+    # each shell has exactly one non-zero contributor, so the rank-order sum is exact
+    return sum_in_rank_order(local, group)
+
+
 def context_evaluator(ctx, mode, tol=1e-10):
     """evaluate(points) on a prepared Context (explicit-point grid, per-point tolerance)."""
     def evaluate(points):

@@ -205,3 +205,24 @@ def folded_records(D):
             ijkl.append((i + 1, j + 1, k + 1, l + 1))
             v.append(s)
     return np.array(ijkl, dtype=np.int32), np.array(v)
+
+
+def batch_workload(n=64, seed=SEED0 + 3, hi=200.0, max_prims=None):
+    """Workload 3: n molecules of 3..20 atoms (random non-overlapping positions, >= 1.8 bohr apart)
+    with 20..300 primitives (l <= 2, exponents up to 200) and uneven closed-shell 1-RDMs
+    (min(electrons / 2, primitives / 3) occupied orbitals). Returns [(index, basis, D)];
+    max_prims keeps only the molecules with at most that many primitives (the others are drawn
+    all the same, so every molecule is the same whatever the subset)."""
+    rng = np.random.default_rng(seed)
+    mols = []
+    for i in range(n):
+        natoms = int(rng.integers(3, 21))
+        nprim = int(rng.integers(20, 301))
+        b = random_molecule(rng, natoms, nprim, hi=hi)
+        nocc = max(1, min(electrons(b) // 2, len(b["alpha"]) // 3))
+        dseed = int(rng.integers(1 << 30))
+        if max_prims is not None and len(b["alpha"]) > max_prims:
+            continue
+        D, _ = closed_shell_density(b, nocc, dseed)
+        mols.append((i, b, D))
+    return mols

@@ -136,3 +136,17 @@ def test_batch_with_d_shells_matches_oracle(ctx, molecules_d):
         np.testing.assert_allclose(a, ref, rtol=1e-11, atol=1e-13 * scale)
         assert np.all(np.abs(m - ref) <= 1e-8 * np.abs(ref) + 1e-12 * scale)
     assert list(counts) == tot.tolist()
+
+
+def test_batch_graph_replay_bit_identical(ctx, molecules):
+    # a prepared batch evaluated through the captured CUDA graph: the capturing call and every
+    # replay give the eager evaluation's bits, and the per-shell I(s) of all molecules follow
+    ctx.batch_clear()
+    for b, D in molecules:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN, nosym=True)
+    ctx.batch_prepare(THRESH)
+    eager = ctx.eval(mode=1, tol=1e-8)
+    per_mol = np.concatenate(ctx.batch_eval(mode=1, tol=1e-8))
+    for _ in range(3):
+        np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+        np.testing.assert_array_equal(ctx.radial_plot()[1], per_mol)

@@ -42,6 +42,24 @@ def test_shard_shells_whole_and_contiguous():
     assert sum(p[1] - p[0] for p in parts) == 2
 
 
+def test_scan_shard_whole_shells():
+    # each rank's share of a scan block is itself a scan block of whole shells; together they
+    # cover every shell once, in order, and gridpoints2 counts the same shells in each share
+    for start, end, step in ((0.0, 10.0, 0.05), (0.0, 5.0, 0.1), (0.5, 3.0, 0.25)):
+        npb = int((end - start) / step) + 1
+        for world in (1, 2, 3, 4, 8):
+            parts = [SH.scan_shard(start, end, step, r, world) for r in range(world)]
+            parts = [p for p in parts if p is not None]
+            assert parts[0][2] == 0 and parts[-1][3] == npb
+            for a, b in zip(parts, parts[1:]):
+                assert a[3] == b[2]
+            for s0, s1, k0, k1 in parts:
+                g = O.gridpoints2([s0], [s1], [step], [26])
+                assert len(g["smn"]) == k1 - k0
+                np.testing.assert_allclose(g["radi"], start + step * np.arange(k0, k1), rtol=0, atol=1e-12)
+    assert SH.scan_shard(0.0, 0.1, 0.1, 0, 4) is None  # more ranks than shells: rank 0 has none
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
