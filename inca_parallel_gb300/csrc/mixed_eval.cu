@@ -492,8 +492,8 @@ __device__ __forceinline__ void load_points(const float4* __restrict__ phi, cons
 //   Its sums only set the estimated thresholds (an estimate that is off costs corrections or a
 //   band pass, never accuracy), so its terms skip the compensation of u (kComp = false) and are
 //   summed in plain FP32, moved to FP64 after every chunk; the error bounds are the same.
-template <bool kFuse, bool kEst = false>
-__global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
+template <bool kFuse, bool kEst = false, int kCtas = INCA_PASS_CTAS_PER_SM, bool kWaitTest = false>
+__global__ void __launch_bounds__(32, kCtas)
 k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
         const float4* __restrict__ plo, const TileInfo* __restrict__ tiles, const float* __restrict__ wtbox,
@@ -503,10 +503,11 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         unsigned long long* __restrict__ work, unsigned long long* __restrict__ stats, int* __restrict__ err,
         int wait_test) {
   static_assert(!(kFuse && kEst), "the estimate pass has no corrections");
-  // wait_test > 0 (a test of the bounded waits, never in production): no staging copy is
-  // started and every wait gives up after wait_test tries, so the error path runs
-  const bool issue = wait_test == 0;
-  const int wlim = wait_test > 0 ? wait_test : kWaitLimit;
+  // kWaitTest (an instantiation for the test of the bounded waits only): no staging copy is
+  // started and every wait gives up after wait_test tries, so the error path runs. Production
+  // instantiations keep both as constants (as a runtime choice they cost about 3 % of the pass).
+  const bool issue = !kWaitTest;
+  const int wlim = kWaitTest ? wait_test : kWaitLimit;
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kFuse ? kExpTab + 1 : 1];
@@ -1531,9 +1532,10 @@ std::vector<float2> exp2_table() {
 // proportion to its tiles x chunks, about kItemsPerCta work items per resident CTA in total
 // (an item is then small next to the whole pass, so the CTAs finish together).
 std::vector<MolWork> work_table(const std::vector<MolSpan>& sp, const std::vector<ChunkRange>& ch, int num_sms,
-                                int items_per_cta, int64_t* nitems, int64_t* npart, int64_t* ndrop) {
+                                int items_per_cta, int64_t* nitems, int64_t* npart, int64_t* ndrop,
+                                int ctas_per_sm = INCA_PASS_CTAS_PER_SM) {
   const int nmol = static_cast<int>(sp.size());
-  const double target = double(num_sms) * INCA_PASS_CTAS_PER_SM * items_per_cta;
+  const double target = double(num_sms) * ctas_per_sm * items_per_cta;
   double total = 0.0;
   for (int m = 0; m < nmol; ++m) total += double(sp[m].ntiles) * std::max(ch[m].end - ch[m].begin, 0);
   std::vector<MolWork> w(nmol);
@@ -1558,11 +1560,15 @@ std::vector<MolWork> work_table(const std::vector<MolSpan>& sp, const std::vecto
   return w;
 }
 
-// Resident CTAs of a persistent pass launch (one-warp CTAs, INCA_PASS_CTAS_PER_SM per SM).
-unsigned persistent_ctas(int64_t nitems, int num_sms) {
+// Resident CTAs of a persistent pass launch (one-warp CTAs, ctas_per_sm per SM).
+unsigned persistent_ctas(int64_t nitems, int num_sms, int ctas_per_sm = INCA_PASS_CTAS_PER_SM) {
   return static_cast<unsigned>(
-      std::max<int64_t>(1, std::min<int64_t>(nitems, static_cast<int64_t>(num_sms) * INCA_PASS_CTAS_PER_SM)));
+      std::max<int64_t>(1, std::min<int64_t>(nitems, static_cast<int64_t>(num_sms) * ctas_per_sm)));
 }
+
+// The register budgets the one-pass kernel is compiled for (resident one-warp CTAs per SM);
+// the schedule (inca_set_tuning, inca_autotune) picks one.
+bool valid_pass_ctas(int n) { return n == 12 || n == 16 || n == 20; }
 
 }  // namespace
 
@@ -1582,6 +1588,7 @@ double env_knob(const char* name, double dflt, double lo, double hi) {
 struct MixedPlan {
   bool fused = false;
   int mode = 2, nseg = 1, emode = 0, nmol = 1, cheap = 1, wait_test = 0;
+  int ctas = INCA_PASS_CTAS_PER_SM;  // resident CTAs per SM of the one-pass kernel (its register budget)
   bool f64 = false;  // the screened FP64 form (k_pass_f64 instead of the FP32 passes)
   const int* seg_of = nullptr;
   int64_t ngrid = 0, nwt = 0, ngroups = 0, nitems = 0, npart = 0, ndrop = 0;
@@ -1621,10 +1628,11 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   P.nwt = c->ntiles;
   P.ngroups = P.nwt * kPPT;
   const int ipc = c->tune_items_per_cta > 0 ? c->tune_items_per_cta : kItemsPerCta;
+  P.ctas = valid_pass_ctas(c->tune_ctas) && P.fused ? c->tune_ctas : INCA_PASS_CTAS_PER_SM;
   const std::vector<MolWork> hmw =
-      work_table(c->mol_span, c->mol_chunks, c->num_sms, ipc, &P.nitems, &P.npart, &P.ndrop);
+      work_table(c->mol_span, c->mol_chunks, c->num_sms, ipc, &P.nitems, &P.npart, &P.ndrop, P.ctas);
   P.nmol = static_cast<int>(hmw.size());
-  P.nctas = persistent_ctas(P.nitems, c->num_sms);
+  P.nctas = persistent_ctas(P.nitems, c->num_sms, P.ctas);
   std::vector<MolWork> hmw_s;
   if (P.fused) {
     P.ns = c->nsample;
@@ -1744,10 +1752,16 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   // ---- estimates from the grid sample (one-pass form): thresholds and drop thresholds
   if (P.fused) {
     const int64_t ns = P.ns;
-    INCA_LAUNCH(c, (k_pass1<false, true>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws, P.nmol, c->d_classes.p,
-                c->d_rec32.p,
-                c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p, P.nitems_s, P.stage_floats, nullptr,
-                nullptr, nullptr, 0, P.q1, P.qabs, nullptr, P.work + 3, P.stats + 8, P.errw, P.wait_test);
+#define INCA_PASS1_EST(T)                                                                                         \
+  INCA_LAUNCH(c, (k_pass1<false, true, INCA_PASS_CTAS_PER_SM, T>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws,     \
+              P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p,     \
+              P.nitems_s, P.stage_floats, nullptr, nullptr, nullptr, 0, P.q1, P.qabs, nullptr, P.work + 3,          \
+              P.stats + 8, P.errw, P.wait_test)
+    if (P.wait_test > 0)
+      INCA_PASS1_EST(true);
+    else
+      INCA_PASS1_EST(false);
+#undef INCA_PASS1_EST
     INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.q1, nullptr, P.Iss);
     INCA_LAUNCH(c, k_sum_mol, nblk32(ns), kSumBlock, 0, ns, P.mws, P.nmol, P.qabs, nullptr, P.Mss);
     if (P.mode == 0) {
@@ -1781,14 +1795,34 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
     INCA_LAUNCH(c, k_pass_f64, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, use_drop ? P.ltdrop : nullptr, P.p1,
                 P.pabs, use_drop ? P.dmass : nullptr, P.work, P.stats, P.errw);
-  else if (P.fused)
-    INCA_LAUNCH(c, k_pass1<true>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
-                c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,
-                use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw, P.wait_test);
+  else if (P.fused) {
+#define INCA_PASS1_FUSED(N)                                                                                       \
+  INCA_LAUNCH(c, (k_pass1<true, false, N>), P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,    \
+              c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,      \
+              use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw, P.wait_test)
+    if (P.wait_test > 0)
+      INCA_LAUNCH(c, (k_pass1<true, false, INCA_PASS_CTAS_PER_SM, true>), P.nctas, 32, P.dsmem, c->d_chunks.p,
+                  P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems,
+                  P.stage_floats, P.ptau_est, P.tab, use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass,
+                  P.work, P.stats, P.errw, P.wait_test);
+    else if (P.ctas == 12)
+      INCA_PASS1_FUSED(12);
+    else if (P.ctas == 20)
+      INCA_PASS1_FUSED(20);
+    else
+      INCA_PASS1_FUSED(16);
+#undef INCA_PASS1_FUSED
+  }
   else
-    INCA_LAUNCH(c, k_pass1<false>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,
-                c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
-                nullptr, 0, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw, P.wait_test);
+    if (P.wait_test > 0)
+      INCA_LAUNCH(c, (k_pass1<false, false, INCA_PASS_CTAS_PER_SM, true>), P.nctas, 32, P.dsmem, c->d_chunks.p,
+                  P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems,
+                  P.stage_floats, nullptr, nullptr, nullptr, 0, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw,
+                  P.wait_test);
+    else
+      INCA_LAUNCH(c, k_pass1<false>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,
+                  c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
+                  nullptr, 0, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw, 0);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[2], c->stream));
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
@@ -1959,17 +1993,19 @@ int eval_fp64_screened(inca_ctx* c, double eps, bool* plain) {
 // fastest stays in the context. All candidates meet the tolerance, so the choice changes only
 // the time. On an error the context's previous schedule is restored.
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_out, double* safety_out,
-                   double* drop_out, double* best_ms, double* default_ms) {
+                   double* drop_out, int* ctas_out, double* best_ms, double* default_ms) {
   struct Sched {
     int ipc, stride;
     double safety, drop;
+    int ctas;
   };
-  const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop};
+  const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop, c->tune_ctas};
   auto apply = [&](const Sched& s) {
     c->tune_items_per_cta = s.ipc;
     c->tune_sample_stride = s.stride;
     c->tune_safety = s.safety;
     c->tune_drop = s.drop;
+    c->tune_ctas = s.ctas;
   };
   auto timed = [&](const Sched& s, double* ms) -> int {
     apply(s);
@@ -1986,7 +2022,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     *ms = t[t.size() / 2];
     return INCA_OK;
   };
-  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac};
+  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM};
   double best = 0.0;
   int st = timed(cur, &best);
   if (st) return st;
@@ -1995,6 +2031,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   const int strides[] = {8, 16, 32, 64};
   const double safeties[] = {0.3, 0.5, 0.7};
   const double drops[] = {0.02, 0.05, 0.1, 0.2};
+  const int ctass[] = {12, 16, 20};
   auto consider = [&](Sched s) -> int {
     double ms;
     const int e = timed(s, &ms);
@@ -2006,20 +2043,23 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     return INCA_OK;
   };
   for (int pass = 0; pass < 2; ++pass) {
+    for (int v : ctass)
+      if (v != cur.ctas && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, v}))) return st;
     for (int v : ipcs)
-      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop}))) return st;
+      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop, cur.ctas}))) return st;
     for (int v : strides)
-      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop}))) return st;
+      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop, cur.ctas}))) return st;
     for (double v : safeties)
-      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop}))) return st;
+      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop, cur.ctas}))) return st;
     for (double v : drops)
-      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v}))) return st;
+      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v, cur.ctas}))) return st;
   }
   apply(cur);
   *ipc_out = cur.ipc;
   *stride_out = cur.stride;
   *safety_out = cur.safety;
   *drop_out = cur.drop;
+  *ctas_out = cur.ctas;
   *best_ms = best;
   return INCA_OK;
 }
@@ -2032,7 +2072,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
 static std::vector<double> plan_signature(const inca_ctx* c, const MixedPlan& P) {
   auto a = [](const void* p) { return static_cast<double>(reinterpret_cast<uintptr_t>(p)); };
   std::vector<double> s = {double(P.fused), double(P.mode), double(P.nseg), double(P.emode), double(P.nmol),
-                           double(P.cheap), double(P.wait_test),
+                           double(P.cheap), double(P.wait_test), double(P.ctas),
                            a(P.seg_of), double(P.ngrid), double(P.nwt), double(P.ngroups), double(P.nitems),
                            double(P.npart), double(P.ndrop), double(P.ns), double(P.nitems_s), double(P.npart_s),
                            double(P.nctas), double(P.nctas_s), double(P.gblk), double(P.tblk),

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define INCA_ABI_VERSION 1
+#define INCA_ABI_VERSION 2
 
 /* status codes */
 #define INCA_OK 0
@@ -153,8 +153,10 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 
 /* Schedule of the mixed evaluation: work items per resident CTA of the persistent passes,
  * the stride of the grid sample that estimates the thresholds, the factor applied to the
- * estimates, and the share of the tolerance given to left-out (quartet, tile) pairs
- * (drop_fraction, below 0.5; < 0: the default 0.05). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
+ * estimates, the share of the tolerance given to left-out (quartet, tile) pairs
+ * (drop_fraction, below 0.5; < 0: the default 0.05), and the register budget of the one-pass
+ * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20, one compiled
+ * instantiation each; 0: the default 16). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
  * (median of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
  * context and reports it with the time of the default schedule; the last evaluation's results
  * stay on the device. inca_set_tuning sets a schedule (NULL: the defaults). Every schedule meets
@@ -166,6 +168,7 @@ typedef struct inca_tuning {
   double best_ms;     /* output of inca_autotune */
   double default_ms;  /* output of inca_autotune */
   double drop_fraction;
+  int32_t ctas_per_sm;
 } inca_tuning;
 int inca_autotune(inca_ctx* ctx, double tol, int32_t reps, inca_tuning* chosen);
 int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);

@@ -34,7 +34,7 @@ def test_binding_covers_header():
 
 
 def test_abi_version(lib):
-    assert lib.inca_abi_version() == 1
+    assert lib.inca_abi_version() == 2
 
 
 def test_centercalc_matches_oracle(lib):

@@ -169,14 +169,15 @@ def test_autotune_keeps_tolerance(ctx, scan_fp64):
     assert t["sample_stride"] in (8, 16, 32, 64)
     assert t["estimate_safety"] in (0.3, 0.5, 0.7)
     assert t["drop_fraction"] in (0.02, 0.05, 0.1, 0.2)
+    assert t["ctas_per_sm"] in (12, 16, 20)
     assert 0 < t["best_ms"] <= t["default_ms"]
     try:
         # the tuned schedule stays in the context; every schedule meets the tolerance
         I = _scan_mixed(ctx)
         rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
         assert rel.max() <= 1e-8, rel.max()
-        for ipc, stride, safety, drop in ((4, 32, 0.3, 0.2), (48, 8, 0.7, 0.02)):
-            ctx.set_tuning(ipc, stride, safety, drop)
+        for ipc, stride, safety, drop, ctas in ((4, 32, 0.3, 0.2, 12), (48, 8, 0.7, 0.02, 20), (12, 16, 0.5, 0.05, 16)):
+            ctx.set_tuning(ipc, stride, safety, drop, ctas)
             I = _scan_mixed(ctx)
             rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
             assert rel.max() <= 1e-8, (ipc, stride, safety, rel.max())
