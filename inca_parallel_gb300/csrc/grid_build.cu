@@ -219,30 +219,78 @@ __global__ void k_smear_prep(int64_t n, const double* px, const double* py, cons
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 // Stable compaction of (x, y, z, w, tag) by keep flags, into the context's grid arrays.
-int compact_into(inca_ctx* c, int64_t ncand, DevBuf<double>& x, DevBuf<double>& y, DevBuf<double>& z,
-                 DevBuf<double>& w, DevBuf<int>& tag, DevBuf<uint8_t>& keep, int64_t* nout) {
-  DevBuf<int> nsel;
-  DevBuf<unsigned char> tmp;
-  if (nsel.reserve(1)) return set_error(c, INCA_E_NOMEM, "grid compaction");
-  if (c->d_px.reserve(ncand) || c->d_py.reserve(ncand) || c->d_pz.reserve(ncand) || c->d_w.reserve(ncand) ||
-      c->d_wvee.reserve(ncand) || c->d_cmap.reserve(ncand)) {
-    nsel.release();
-    return set_error(c, INCA_E_NOMEM, "grid arrays");
+// Bump allocation over a context-owned device buffer: a dry run (base == nullptr) measures
+// the bytes, the buffer grows to that (never shrinks), and the same sequence of take() calls
+// carves it. The grid builders' temporaries live there, so rebuilding a grid allocates and
+// frees nothing once the buffer is large enough.
+struct Slab {
+  unsigned char* base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
   }
+};
+
+// Temporaries of a grid build: candidate points, weights, tags, keep flags, the selected count
+// and the stream-compaction's temporary storage.
+struct Candidates {
+  double *x, *y, *z, *w;
+  int* tag;
+  uint8_t* keep;
+  int* nsel;
+  unsigned char* tmp;
+  size_t tmp_bytes;
+};
+
+// Carve the candidate arrays for ncand points (plus `extra`, which carves the caller's own
+// tables from the same slab) out of the context's grid scratch.
+template <typename Extra>
+int carve_candidates(inca_ctx* c, int64_t ncand, Candidates& cd, Extra&& extra) {
   size_t tb = 0;
-  cudaError_t e = cub::DeviceSelect::Flagged(nullptr, tb, x.p, keep.p, c->d_px.p, nsel.p, ncand, c->stream);
-  if (e == cudaSuccess) e = tmp.reserve(tb);
+  cudaError_t e = cub::DeviceSelect::Flagged(nullptr, tb, static_cast<const double*>(nullptr),
+                                             static_cast<const uint8_t*>(nullptr), static_cast<double*>(nullptr),
+                                             static_cast<int*>(nullptr), ncand, c->stream);
+  if (e) return cuda_error(c, e, "grid compaction");
+  auto layout = [&](Slab& sl) {
+    cd.x = sl.take<double>(ncand);
+    cd.y = sl.take<double>(ncand);
+    cd.z = sl.take<double>(ncand);
+    cd.w = sl.take<double>(ncand);
+    cd.tag = sl.take<int>(ncand);
+    cd.keep = sl.take<uint8_t>(ncand);
+    cd.nsel = sl.take<int>(1);
+    cd.tmp = sl.take<unsigned char>(tb);
+    cd.tmp_bytes = tb;
+    extra(sl);
+  };
+  Slab dry;
+  layout(dry);
+  if (c->d_gscratch.reserve(dry.off + 256)) return set_error(c, INCA_E_NOMEM, "grid scratch");
+  Slab sl{c->d_gscratch.p};
+  layout(sl);
+  return INCA_OK;
+}
+
+// Keep the flagged candidates (in order) as the context's grid arrays; *nout gets their count.
+int compact_into(inca_ctx* c, int64_t ncand, const Candidates& cd, int64_t* nout) {
+  if (c->d_px.reserve(ncand) || c->d_py.reserve(ncand) || c->d_pz.reserve(ncand) || c->d_w.reserve(ncand) ||
+      c->d_wvee.reserve(ncand) || c->d_cmap.reserve(ncand))
+    return set_error(c, INCA_E_NOMEM, "grid arrays");
+  size_t tb = cd.tmp_bytes;
+  cudaError_t e = cudaSuccess;
   double* outs[4] = {c->d_px.p, c->d_py.p, c->d_pz.p, c->d_w.p};
-  double* ins[4] = {x.p, y.p, z.p, w.p};
+  const double* ins[4] = {cd.x, cd.y, cd.z, cd.w};
   for (int k = 0; k < 4 && e == cudaSuccess; ++k)
-    e = cub::DeviceSelect::Flagged(tmp.p, tb, ins[k], keep.p, outs[k], nsel.p, ncand, c->stream);
+    e = cub::DeviceSelect::Flagged(cd.tmp, tb, ins[k], cd.keep, outs[k], cd.nsel, ncand, c->stream);
   if (e == cudaSuccess)
-    e = cub::DeviceSelect::Flagged(tmp.p, tb, tag.p, keep.p, c->d_cmap.p, nsel.p, ncand, c->stream);
+    e = cub::DeviceSelect::Flagged(cd.tmp, tb, cd.tag, cd.keep, c->d_cmap.p, cd.nsel, ncand, c->stream);
   int h = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, nsel.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, cd.nsel, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  nsel.release();
-  tmp.release();
   if (e != cudaSuccess) return cuda_error(c, e, "grid compaction");
   *nout = h;
   return INCA_OK;
@@ -287,42 +335,40 @@ int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nang
     lw.insert(lw.end(), w.begin(), w.end());
     ncand += static_cast<int64_t>(nradc[q]) * nangc[q];
   }
-  DevBuf<RadialCentre> dcen;
-  DevBuf<double> drad, dwr, dlx, dly, dlz, dlw, cx, cy, cz, cw;
-  DevBuf<int> ctag;
-  DevBuf<uint8_t> keep;
-  auto rel = [&]() {
-    dcen.release(); drad.release(); dwr.release(); dlx.release(); dly.release(); dlz.release(); dlw.release();
-    cx.release(); cy.release(); cz.release(); cw.release(); ctag.release(); keep.release();
-  };
-  if (dcen.reserve(nquad) || drad.reserve(radius.size()) || dwr.reserve(wrad.size()) || dlx.reserve(lx.size()) ||
-      dly.reserve(ly.size()) || dlz.reserve(lz.size()) || dlw.reserve(lw.size()) || cx.reserve(ncand) ||
-      cy.reserve(ncand) || cz.reserve(ncand) || cw.reserve(ncand) || ctag.reserve(ncand) || keep.reserve(ncand)) {
-    rel();
-    return set_error(c, INCA_E_NOMEM, "inca_grid_radial");
-  }
-  cudaError_t e = cudaMemcpyAsync(dcen.p, cen.data(), sizeof(RadialCentre) * nquad, cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(drad.p, radius.data(), sizeof(double) * radius.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dwr.p, wrad.data(), sizeof(double) * wrad.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlx.p, lx.data(), sizeof(double) * lx.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dly.p, ly.data(), sizeof(double) * ly.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlz.p, lz.data(), sizeof(double) * lz.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlw.p, lw.data(), sizeof(double) * lw.size(), cudaMemcpyHostToDevice, c->stream);
+  const size_t nlx = lx.size(), nrr = radius.size();
+  RadialCentre* dcen = nullptr;
+  double *drad = nullptr, *dwr = nullptr, *dlx = nullptr, *dly = nullptr, *dlz = nullptr, *dlw = nullptr;
+  double *dR = nullptr, *dchi = nullptr, *dcent = nullptr;
+  Candidates cd;
+  int st = carve_candidates(c, ncand, cd, [&](Slab& sl) {
+    dcen = sl.take<RadialCentre>(nquad);
+    drad = sl.take<double>(nrr);
+    dwr = sl.take<double>(nrr);
+    dlx = sl.take<double>(nlx);
+    dly = sl.take<double>(nlx);
+    dlz = sl.take<double>(nlx);
+    dlw = sl.take<double>(nlx);
+    dR = sl.take<double>(static_cast<size_t>(nquad) * nquad);
+    dchi = sl.take<double>(static_cast<size_t>(nquad) * nquad);
+    dcent = sl.take<double>(3 * static_cast<size_t>(nquad));
+  });
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(dcen, cen.data(), sizeof(RadialCentre) * nquad, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(drad, radius.data(), sizeof(double) * nrr, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dwr, wrad.data(), sizeof(double) * nrr, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlx, lx.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dly, ly.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlz, lz.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlw, lw.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
   if (!e) {
-    INCA_LAUNCH(c, k_radial_candidates, nblk(ncand), 256, 0, ncand, dcen.p, nquad, drad.p, dwr.p, dlx.p, dly.p, dlz.p,
-                                                            dlw.p, nosym, cx.p, cy.p, cz.p, cw.p, ctag.p, keep.p);
+    INCA_LAUNCH(c, k_radial_candidates, nblk(ncand), 256, 0, ncand, dcen, nquad, drad, dwr, dlx, dly, dlz, dlw,
+                nosym, cd.x, cd.y, cd.z, cd.w, cd.tag, cd.keep);
     e = cudaGetLastError();
   }
-  if (e) {
-    rel();
-    return cuda_error(c, e, "inca_grid_radial (candidates)");
-  }
+  if (e) return cuda_error(c, e, "inca_grid_radial (candidates)");
   int64_t rgrid = 0;
-  int st = compact_into(c, ncand, cx, cy, cz, cw, ctag, keep, &rgrid);
-  if (st) {
-    rel();
-    return st;
-  }
+  st = compact_into(c, ncand, cd, &rgrid);
+  if (st) return st;
   int64_t ngrid = rgrid;
   if (nquad > 1) {
     std::vector<double> Rij(nquad * nquad), chi(nquad * nquad);
@@ -333,46 +379,31 @@ int grid_radial_device(inca_ctx* c, int nquad, const int* nradc, const int* nang
         Rij[i * nquad + j] = std::sqrt(s);
         chi[i * nquad + j] = Ps[j] > 1e-12 ? std::pow(Ps[i] / Ps[j], 1.0 / 3.0) : 1.0;
       }
-    DevBuf<double> dR, dchi, dcent;
-    if (dR.reserve(Rij.size()) || dchi.reserve(chi.size()) || dcent.reserve(3 * nquad)) {
-      rel();
-      return set_error(c, INCA_E_NOMEM, "tfvc");
-    }
-    e = cudaMemcpyAsync(dR.p, Rij.data(), sizeof(double) * Rij.size(), cudaMemcpyHostToDevice, c->stream);
-    if (!e) e = cudaMemcpyAsync(dchi.p, chi.data(), sizeof(double) * chi.size(), cudaMemcpyHostToDevice, c->stream);
-    if (!e) e = cudaMemcpyAsync(dcent.p, cent, sizeof(double) * 3 * nquad, cudaMemcpyHostToDevice, c->stream);
+    e = cudaMemcpyAsync(dR, Rij.data(), sizeof(double) * Rij.size(), cudaMemcpyHostToDevice, c->stream);
+    if (!e) e = cudaMemcpyAsync(dchi, chi.data(), sizeof(double) * chi.size(), cudaMemcpyHostToDevice, c->stream);
+    if (!e) e = cudaMemcpyAsync(dcent, cent, sizeof(double) * 3 * nquad, cudaMemcpyHostToDevice, c->stream);
     if (!e) {
       const unsigned tb = nblk(rgrid, 128);
-      INCA_LAUNCH(c, k_tfvc, tb, 128, 0, rgrid, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_cmap.p, nquad, dcent.p, dR.p,
-                  dchi.p, c->d_w.p);
+      INCA_LAUNCH(c, k_tfvc, tb, 128, 0, rgrid, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_cmap.p, nquad, dcent, dR, dchi,
+                  c->d_w.p);
       e = cudaGetLastError();
     }
     if (!e) {
       // copy the weighted grid back to candidates and drop weights <= 1e-106
-      e = cudaMemcpyAsync(cx.p, c->d_px.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
-      if (!e) e = cudaMemcpyAsync(cy.p, c->d_py.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
-      if (!e) e = cudaMemcpyAsync(cz.p, c->d_pz.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
-      if (!e) e = cudaMemcpyAsync(cw.p, c->d_w.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
-      if (!e) e = cudaMemcpyAsync(ctag.p, c->d_cmap.p, sizeof(int) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
+      e = cudaMemcpyAsync(cd.x, c->d_px.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
+      if (!e) e = cudaMemcpyAsync(cd.y, c->d_py.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
+      if (!e) e = cudaMemcpyAsync(cd.z, c->d_pz.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
+      if (!e) e = cudaMemcpyAsync(cd.w, c->d_w.p, sizeof(double) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
+      if (!e) e = cudaMemcpyAsync(cd.tag, c->d_cmap.p, sizeof(int) * rgrid, cudaMemcpyDeviceToDevice, c->stream);
       if (!e) {
-        INCA_LAUNCH(c, k_weight_keep, nblk(rgrid), 256, 0, rgrid, cw.p, keep.p);
+        INCA_LAUNCH(c, k_weight_keep, nblk(rgrid), 256, 0, rgrid, cd.w, cd.keep);
         e = cudaGetLastError();
       }
     }
-    dR.release();
-    dchi.release();
-    dcent.release();
-    if (e) {
-      rel();
-      return cuda_error(c, e, "inca_grid_radial (tfvc)");
-    }
-    st = compact_into(c, rgrid, cx, cy, cz, cw, ctag, keep, &ngrid);
-    if (st) {
-      rel();
-      return st;
-    }
+    if (e) return cuda_error(c, e, "inca_grid_radial (tfvc)");
+    st = compact_into(c, rgrid, cd, &ngrid);
+    if (st) return st;
   }
-  rel();
   INCA_LAUNCH(c, k_vee, nblk(ngrid), 256, 0, ngrid, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_w.p, c->d_wvee.p);
   INCA_CUDA(c, cudaGetLastError());
   INCA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -417,37 +448,31 @@ int grid_scan_device(inca_ctx* c, int nblock, const double* start, const double*
   }
   const int nsh = static_cast<int>(sh.size());
   if (nsh == 0) return set_error(c, INCA_E_ARG, "inca_grid_scan: no shells");
-  DevBuf<ScanShell> dsh;
-  DevBuf<double> dlx, dly, dlz, dlw, cx, cy, cz, cw;
-  DevBuf<int> ctag;
-  DevBuf<uint8_t> keep;
-  auto rel = [&]() {
-    dsh.release(); dlx.release(); dly.release(); dlz.release(); dlw.release();
-    cx.release(); cy.release(); cz.release(); cw.release(); ctag.release(); keep.release();
-  };
-  if (dsh.reserve(nsh) || dlx.reserve(lx.size()) || dly.reserve(ly.size()) || dlz.reserve(lz.size()) ||
-      dlw.reserve(lw.size()) || cx.reserve(ncand) || cy.reserve(ncand) || cz.reserve(ncand) || cw.reserve(ncand) ||
-      ctag.reserve(ncand) || keep.reserve(ncand)) {
-    rel();
-    return set_error(c, INCA_E_NOMEM, "inca_grid_scan");
-  }
-  cudaError_t e = cudaMemcpyAsync(dsh.p, sh.data(), sizeof(ScanShell) * nsh, cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlx.p, lx.data(), sizeof(double) * lx.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dly.p, ly.data(), sizeof(double) * ly.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlz.p, lz.data(), sizeof(double) * lz.size(), cudaMemcpyHostToDevice, c->stream);
-  if (!e) e = cudaMemcpyAsync(dlw.p, lw.data(), sizeof(double) * lw.size(), cudaMemcpyHostToDevice, c->stream);
+  const size_t nlx = lx.size();
+  ScanShell* dsh = nullptr;
+  double *dlx = nullptr, *dly = nullptr, *dlz = nullptr, *dlw = nullptr;
+  Candidates cd;
+  int st = carve_candidates(c, ncand, cd, [&](Slab& sl) {
+    dsh = sl.take<ScanShell>(nsh);
+    dlx = sl.take<double>(nlx);
+    dly = sl.take<double>(nlx);
+    dlz = sl.take<double>(nlx);
+    dlw = sl.take<double>(nlx);
+  });
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(dsh, sh.data(), sizeof(ScanShell) * nsh, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlx, lx.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dly, ly.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlz, lz.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
+  if (!e) e = cudaMemcpyAsync(dlw, lw.data(), sizeof(double) * nlx, cudaMemcpyHostToDevice, c->stream);
   if (!e) {
-    INCA_LAUNCH(c, k_scan_candidates, nblk(ncand), 256, 0, ncand, dsh.p, nsh, dlx.p, dly.p, dlz.p, dlw.p, nosym, cx.p,
-                                                          cy.p, cz.p, cw.p, ctag.p, keep.p);
+    INCA_LAUNCH(c, k_scan_candidates, nblk(ncand), 256, 0, ncand, dsh, nsh, dlx, dly, dlz, dlw, nosym, cd.x, cd.y,
+                cd.z, cd.w, cd.tag, cd.keep);
     e = cudaGetLastError();
   }
-  if (e) {
-    rel();
-    return cuda_error(c, e, "inca_grid_scan");
-  }
+  if (e) return cuda_error(c, e, "inca_grid_scan");
   int64_t n = 0;
-  const int st = compact_into(c, ncand, cx, cy, cz, cw, ctag, keep, &n);
-  rel();
+  st = compact_into(c, ncand, cd, &n);
   if (st) return st;
   // points per shell: the shell tags are sorted, count on the host from the Lebedev z's
   c->h_smn.assign(nsh, 0);

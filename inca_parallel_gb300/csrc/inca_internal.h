@@ -183,6 +183,12 @@ struct inca_ctx {
   inca::DevBuf<double> d_px, d_py, d_pz, d_w, d_wvee;
   inca::DevBuf<int> d_cmap;
   inca::DevBuf<double> d_ivec;
+  // temporaries of the grid builders (candidates, tables, compaction), kept between calls
+  inca::DevBuf<unsigned char> d_gscratch;
+  // temporaries of the Morton sort of the mixed form (keys, indices, radix-sort storage, bounding
+  // box), kept between calls
+  inca::DevBuf<unsigned char> d_sscratch;
+  inca::DevBuf<double> d_bbox;
   // scratch of the per-shell / per-centre reductions (segment offsets, sums), kept between calls
   inca::DevBuf<int64_t> d_roff;
   inca::DevBuf<double> d_rsum;

@@ -1095,6 +1095,30 @@ __global__ void k_gather_points(int64_t n, const int64_t* __restrict__ perm, con
   plo[i] = make_float4(l[0], l[1], l[2], 0.0f);
 }
 
+// Bounding box of n points (min x, y, z then max x, y, z), one block of 1024 threads: each
+// thread strides over the points, then a shared-memory tree (min and max are exact, so the
+// result does not depend on the order).
+__global__ void __launch_bounds__(1024) k_bbox(int64_t n, const double* __restrict__ px, const double* __restrict__ py,
+                                               const double* __restrict__ pz, double* out) {
+  __shared__ double sh[6][1024];
+  double v[6] = {HUGE_VAL, HUGE_VAL, HUGE_VAL, -HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+  for (int64_t g = threadIdx.x; g < n; g += blockDim.x) {
+    const double x = px[g], y = py[g], z = pz[g];
+    v[0] = fmin(v[0], x); v[1] = fmin(v[1], y); v[2] = fmin(v[2], z);
+    v[3] = fmax(v[3], x); v[4] = fmax(v[4], y); v[5] = fmax(v[5], z);
+  }
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int k = 0; k < 6; ++k)
+        sh[k][threadIdx.x] = k < 3 ? fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + h])
+                                   : fmax(sh[k][threadIdx.x], sh[k][threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
 // Bounding boxes (FP32, rounded outwards) of each 128-point tile and its four 32-point
 // sub-tiles (points lane + 32 p). One warp per tile.
 __global__ void k_boxes(const TileInfo* __restrict__ tiles, int64_t nwt, const float4* __restrict__ phi,
@@ -1403,6 +1427,19 @@ __global__ void k_thr_exact_max(const unsigned long long* __restrict__ mx, const
 
 inline unsigned nblk(int64_t n, int bs = 256) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
+// Bump allocator over a scratch buffer: a dry run (base == nullptr) measures the size.
+struct Carve {
+  unsigned char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
 // permutation (sorted position -> grid index) and the tile / sub-tile boxes.
 int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, DevBuf<float4>& phi,
@@ -1431,28 +1468,36 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
   if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT) ||
       tiles.reserve(std::max<int64_t>(nwt, 1)))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
-  if (nwt) INCA_CUDA(c, cudaMemcpy(tiles.p, ht.data(), sizeof(TileInfo) * nwt, cudaMemcpyHostToDevice));
-  DevBuf<uint64_t> k1, k2;
-  DevBuf<int64_t> i1;
-  DevBuf<unsigned char> tmp;
-  auto rel = [&]() { k1.release(); k2.release(); i1.release(); tmp.release(); };
-  if (k1.reserve(n) || k2.reserve(n) || i1.reserve(n)) {
-    rel();
-    return set_error(c, INCA_E_NOMEM, "morton sort");
-  }
-  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p,
-              batch ? c->d_pmol.p : nullptr, lo[0], lo[1], lo[2], inv, k1.p, i1.p);
+  if (nwt) INCA_CUDA(c, cudaMemcpyAsync(tiles.p, ht.data(), sizeof(TileInfo) * nwt, cudaMemcpyHostToDevice, c->stream));
+  // keys, indices and the radix sort's storage in the context's sort scratch (kept between calls)
   size_t tb = 0;
-  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
-  if (!e) e = tmp.reserve(tb);
-  if (!e) e = cub::DeviceRadixSort::SortPairs(tmp.p, tb, k1.p, k2.p, i1.p, perm.p, n, 0, 63, c->stream);
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb, static_cast<uint64_t*>(nullptr),
+                                                  static_cast<uint64_t*>(nullptr), static_cast<int64_t*>(nullptr),
+                                                  static_cast<int64_t*>(nullptr), n, 0, 63, c->stream);
+  if (e) return cuda_error(c, e, "morton sort");
+  uint64_t *k1 = nullptr, *k2 = nullptr;
+  int64_t* i1 = nullptr;
+  unsigned char* tmp = nullptr;
+  auto layout = [&](Carve& cv) {
+    k1 = cv.take<uint64_t>(n);
+    k2 = cv.take<uint64_t>(n);
+    i1 = cv.take<int64_t>(n);
+    tmp = cv.take<unsigned char>(tb);
+  };
+  Carve dry{nullptr};
+  layout(dry);
+  if (c->d_sscratch.reserve(dry.off + 256)) return set_error(c, INCA_E_NOMEM, "morton sort");
+  Carve cv{c->d_sscratch.p};
+  layout(cv);
+  INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p,
+              batch ? c->d_pmol.p : nullptr, lo[0], lo[1], lo[2], inv, k1, i1);
+  e = cub::DeviceRadixSort::SortPairs(tmp, tb, k1, k2, i1, perm.p, n, 0, 63, c->stream);
   if (!e) {
     INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, phi.p, plo.p);
     INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p,
                 boxes.p + 8 * nwt);
-    e = cudaStreamSynchronize(c->stream);
+    e = cudaStreamSynchronize(c->stream);  // the host tile table above is stack-owned
   }
-  rel();
   if (e) return cuda_error(c, e, "sorted grid");
   *n_out = n;
   *ntiles_out = nwt;
@@ -1466,17 +1511,13 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
   const bool sample_ok = !sample || (c->sample_version == c->grid_version && c->sample_stride_built == stride);
   if (main_ok && sample_ok) return INCA_OK;
   const int64_t n = c->ngrid;
-  // bounding box of the grid (one host copy of the coordinates; cheap next to evaluation)
-  std::vector<double> hx(n), hy(n), hz(n);
-  INCA_CUDA(c, cudaMemcpy(hx.data(), c->d_px.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  INCA_CUDA(c, cudaMemcpy(hy.data(), c->d_py.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  INCA_CUDA(c, cudaMemcpy(hz.data(), c->d_pz.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
-  for (int64_t g = 0; g < n; ++g) {
-    lo[0] = std::min(lo[0], hx[g]); hi[0] = std::max(hi[0], hx[g]);
-    lo[1] = std::min(lo[1], hy[g]); hi[1] = std::max(hi[1], hy[g]);
-    lo[2] = std::min(lo[2], hz[g]); hi[2] = std::max(hi[2], hz[g]);
-  }
+  // bounding box of the grid, reduced on the device (six values come back)
+  if (c->d_bbox.reserve(6)) return set_error(c, INCA_E_NOMEM, "bounding box");
+  INCA_LAUNCH(c, k_bbox, 1, 1024, 0, n, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_bbox.p);
+  double bb[6];
+  INCA_CUDA(c, cudaMemcpyAsync(bb, c->d_bbox.p, sizeof(bb), cudaMemcpyDeviceToHost, c->stream));
+  INCA_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double lo[3] = {bb[0], bb[1], bb[2]}, hi[3] = {bb[3], bb[4], bb[5]};
   const double ext = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-12));
   const double inv = 2097151.0 / ext;
   int64_t nn = 0;
@@ -1496,18 +1537,6 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
   return INCA_OK;
 }
 
-// Bump allocator over a scratch buffer: a dry run (base == nullptr) measures the size.
-struct Carve {
-  unsigned char* base;
-  size_t off = 0;
-  template <typename T>
-  T* take(size_t n) {
-    off = (off + 255) & ~size_t(255);
-    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
-    off += n * sizeof(T);
-    return p;
-  }
-};
 
 struct Events {
   cudaEvent_t e[6] = {};

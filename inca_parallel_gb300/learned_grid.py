@@ -334,6 +334,48 @@ def judge_equal_points(lg, cases, nrads=(30, 50), nang=302, dense=(150, 974), ct
     return out
 
 
+LEVELS = ((10, 26), (15, 50), (20, 86), (30, 146), (40, 194), (50, 302), (75, 434), (100, 590))
+
+
+def level_study(ctx, nmol=20, seed=4242, levels=LEVELS, auto=(50, 302), dense=(150, 974)):
+    """What any per-centre choice of (nrad, nang) could gain over autogrid's uniform grid.
+
+    For each seeded molecule (2-8 atoms, s and p primitives, real closed-shell DM2) every centre's
+    TFVC component of the radial integral is computed on the dense grid and at every level
+    (one grid per level serves all centres: a component depends only on its own centre's grid).
+    The best possible allocation with a per-centre error budget of autogrid's error / centres is
+    then read off the table -- an upper bound of what a predictor of per-centre levels can do.
+    Returns one dict per molecule: autogrid's relative error, the allocation's relative error
+    and its points relative to autogrid's."""
+    from . import centercalc
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nmol):
+        b, D = _judge_molecule(rng, natoms_range=(2, 9), nprim_range=(10, 60))
+        ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
+        ctx.gen_closed_shell_dm2(D, unique=True)
+        ctx.prepare(1e-12)
+        cent, Ps, alf = centercalc(b["an"], b["cartes"])
+        nc = len(Ps)
+        tot_ref, ref, _ = centre_components(ctx, cent, Ps, alf, *dense)
+        comps, pts = [], []
+        for nr, na in levels:
+            _, pc, ng = centre_components(ctx, cent, Ps, alf, nr, na)
+            comps.append(pc)
+            pts.append(ng / nc)
+        comps = np.asarray(comps)
+        err = np.abs(comps - ref[None, :])
+        ia = list(levels).index(tuple(auto))
+        auto_err = abs(comps[ia].sum() - tot_ref)
+        budget = max(auto_err, 1e-300) / nc
+        k = [next((i for i in range(len(levels)) if err[i, c] <= budget), len(levels) - 1) for c in range(nc)]
+        alloc = abs(sum(comps[k[c], c] for c in range(nc)) - tot_ref)
+        out.append({"centres": nc, "auto_rel_err": auto_err / abs(tot_ref), "alloc_rel_err": alloc / abs(tot_ref),
+                    "alloc_points_rel": sum(pts[i] for i in k) / (pts[ia] * nc),
+                    "levels": np.bincount(k, minlength=len(levels)).tolist()})
+    return out
+
+
 def main(argv=None):
     """Train on autogrid's centres for 500 seeded geometries of 2-20 atoms and judge the learned
     grids against dense grids (nrad 150, nang 974) on held-out molecules with real DM2s:

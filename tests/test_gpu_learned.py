@@ -97,3 +97,15 @@ def test_per_centre_dense_grid_targets():
         assert errs.shape == (len(LG.MULTS), len(Ps))
         best = np.log(np.asarray(LG.MULTS))[np.argmin(errs, axis=0)]
         np.testing.assert_array_equal(t3, best)
+
+
+def test_level_study_runs():
+    # the study behind the learned-grid conclusion: per-centre (nrad, nang) levels against the
+    # dense grid; every molecule gets finite errors and a point count for the best allocation
+    from inca_parallel_gb300 import Context
+    with Context(0) as ctx:
+        res = LG.level_study(ctx, nmol=3)
+    assert len(res) == 3
+    for r in res:
+        assert r["centres"] >= 1 and sum(r["levels"]) == r["centres"]
+        assert np.isfinite(r["auto_rel_err"]) and np.isfinite(r["alloc_rel_err"]) and r["alloc_points_rel"] > 0
