@@ -1,5 +1,7 @@
 """The network's GPU kernels (inca_mlp_*) against the numpy reference, deterministic training,
-and what the trained predictor gains over autogrid's radial scales on held-out molecules.
+what the trained predictor gains over autogrid's radial scales on held-out centres in the 1D
+radial objective it is trained for (not in the 3D radial integral, where no learned grid gains:
+see learned_grid.level_study), and that study itself.
 
 Tolerances: forward 1e-5 and gradient 1e-4 relative to the largest value (FP32 kernels against
 the float64 reference); training is bit-reproducible for a given seed.
