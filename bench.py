@@ -428,7 +428,7 @@ def gpu_arm(args):
     # bind(C) shim), tuned schedule;
     # the quartet input and the I(r) output live in pinned host memory
     ctx.set_tuning(sched["items_per_cta"], sched["sample_stride"], sched["estimate_safety"], sched["drop_fraction"],
-                   sched["ctas_per_sm"])
+                   sched["ctas_per_sm"], sched["cheap_slack"])
     ctx.grid_scan(*scan_args)
     pin_ijkl = torch.empty(ijkl.size, dtype=torch.int32, pin_memory=True).numpy()
     pin_v = torch.empty(v.size, dtype=torch.float64, pin_memory=True).numpy()
@@ -521,6 +521,7 @@ def gpu_arm(args):
                                     "items_per_cta": sched["items_per_cta"], "sample_stride": sched["sample_stride"],
                                     "estimate_safety": sched["estimate_safety"],
                                     "drop_fraction": sched["drop_fraction"], "ctas_per_sm": sched["ctas_per_sm"],
+                                    "cheap_slack": sched["cheap_slack"],
                                     "default_ms": sched["default_ms"],
                                     "tuned_ms": sched["best_ms"], "tuning_s": t_tune},
                        "radial_integral_nrad50_nang110": {"fp64_ms": ri["fp64"]["ms"], "mixed_ms": ri["mixed"]["ms"],

@@ -236,6 +236,7 @@ struct inca_ctx {
   double tune_safety = -1.0;
   double tune_drop = -1.0;
   int tune_ctas = 0;  // resident CTAs per SM of the one-pass kernel (0: the default)
+  int tune_cheap_slack = -1;  // cheap-tier slack in powers of two (-1: the default, 0)
   int sample_stride_built = 0;  // stride of the current sorted sample
 
   // graph replay of the mixed evaluation (captured for one grid, set of records and tolerance)
@@ -264,7 +265,7 @@ int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int b
 int eval_device(inca_ctx* c, int mode, double tol, bool graph = false);
 // mixed_eval.cu
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc, int* stride, double* safety, double* drop,
-                   int* ctas, double* best_ms, double* default_ms);
+                   int* ctas, int* slack, double* best_ms, double* default_ms);
 int ensure_exp_table(inca_ctx* c);
 // cube_eval.cu
 bool cube_separable(const inca_ctx* c);

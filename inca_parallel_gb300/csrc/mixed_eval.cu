@@ -587,7 +587,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       uint32_t mc = 0u;
       if (kFuse && lt_drop && cheap_tier) {
         const float lc = live ? cheap_log2_err(st + lane * rs, L, box, lb) : HUGE_VALF;
-        const bool cheap = lc <= thr;
+        const bool cheap = lc <= thr + static_cast<float>(cheap_tier - 1);
         mc = __ballot_sync(0xffffffffu, cheap);
         if (cheap) dm += exp2f(lc);
       }
@@ -975,7 +975,8 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       // pairs of the one-pass kernel's cheap tier (same decision): their error is bounded
       // within the left-out mass, nothing to correct
       const bool cheap =
-          lt_drop && cheap_tier && lane < w.count && lb > thr && cheap_log2_err(Rq, L, wbox, lb) <= thr;
+          lt_drop && cheap_tier && lane < w.count && lb > thr &&
+          cheap_log2_err(Rq, L, wbox, lb) <= thr + static_cast<float>(cheap_tier - 1);
       const uint32_t live = __ballot_sync(0xffffffffu, lane < w.count && lb > thr && !cheap);
       uint32_t msub[kPPT];
       uint32_t any = 0;
@@ -1649,8 +1650,14 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   P.tau_scale = env_knob("INCA_TAU_SCALE", kTauScale, 1e-300, HUGE_VAL);
   P.drop_frac = env_knob("INCA_DROP_FRACTION", c->tune_drop >= 0.0 ? c->tune_drop : kDropFrac, 0.0, 0.5);
   P.safety = env_knob("INCA_EST_SAFETY", c->tune_safety >= 0.0 ? c->tune_safety : kEstSafety, 0.0, HUGE_VAL);
-  // the cheap tier of the one-pass form (0 evaluates every live pair in compensated FP32)
-  P.cheap = env_knob("INCA_CHEAP_TIER", 1.0, 0.0, 2.0) >= 0.5 ? 1 : 0;
+  // the cheap tier of the one-pass form (0 evaluates every live pair in compensated FP32), and
+  // its slack: a pair takes the tier when its error bound is at most 2^slack times the drop
+  // threshold (0: within the threshold, so the left-out mass keeps its a-priori bound; larger:
+  // checked after the pass like the rest of the left-out mass). Passed to the kernels as
+  // 0 (off) or 1 + slack.
+  const int slack = static_cast<int>(env_knob("INCA_CHEAP_SLACK", c->tune_cheap_slack >= 0 ? c->tune_cheap_slack : 0,
+                                              0.0, 31.0));
+  P.cheap = env_knob("INCA_CHEAP_TIER", 1.0, 0.0, 2.0) >= 0.5 ? 1 + slack : 0;
   // test of the bounded staging waits: the pass-1 kernels start no copy and give up waiting
   // after this many tries (0: off)
   P.wait_test = static_cast<int>(env_knob("INCA_TEST_STAGE_TIMEOUT", 0.0, 0.0, 1e6));
@@ -2022,19 +2029,21 @@ int eval_fp64_screened(inca_ctx* c, double eps, bool* plain) {
 // fastest stays in the context. All candidates meet the tolerance, so the choice changes only
 // the time. On an error the context's previous schedule is restored.
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_out, double* safety_out,
-                   double* drop_out, int* ctas_out, double* best_ms, double* default_ms) {
+                   double* drop_out, int* ctas_out, int* slack_out, double* best_ms, double* default_ms) {
   struct Sched {
     int ipc, stride;
     double safety, drop;
-    int ctas;
+    int ctas, slack;
   };
-  const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop, c->tune_ctas};
+  const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop, c->tune_ctas,
+                    c->tune_cheap_slack};
   auto apply = [&](const Sched& s) {
     c->tune_items_per_cta = s.ipc;
     c->tune_sample_stride = s.stride;
     c->tune_safety = s.safety;
     c->tune_drop = s.drop;
     c->tune_ctas = s.ctas;
+    c->tune_cheap_slack = s.slack;
   };
   auto timed = [&](const Sched& s, double* ms) -> int {
     apply(s);
@@ -2051,7 +2060,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     *ms = t[t.size() / 2];
     return INCA_OK;
   };
-  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM};
+  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, 0};
   double best = 0.0;
   int st = timed(cur, &best);
   if (st) return st;
@@ -2061,6 +2070,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   const double safeties[] = {0.3, 0.5, 0.7};
   const double drops[] = {0.02, 0.05, 0.1, 0.2};
   const int ctass[] = {12, 16, 20};
+  const int slacks[] = {0, 2, 4, 6, 8};
   auto consider = [&](Sched s) -> int {
     double ms;
     const int e = timed(s, &ms);
@@ -2073,15 +2083,17 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   };
   for (int pass = 0; pass < 2; ++pass) {
     for (int v : ctass)
-      if (v != cur.ctas && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, v}))) return st;
+      if (v != cur.ctas && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, v, cur.slack}))) return st;
     for (int v : ipcs)
-      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop, cur.ctas}))) return st;
+      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop, cur.ctas, cur.slack}))) return st;
     for (int v : strides)
-      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop, cur.ctas}))) return st;
+      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop, cur.ctas, cur.slack}))) return st;
     for (double v : safeties)
-      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop, cur.ctas}))) return st;
+      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop, cur.ctas, cur.slack}))) return st;
     for (double v : drops)
-      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v, cur.ctas}))) return st;
+      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v, cur.ctas, cur.slack}))) return st;
+    for (int v : slacks)
+      if (v != cur.slack && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, cur.ctas, v}))) return st;
   }
   apply(cur);
   *ipc_out = cur.ipc;
@@ -2089,6 +2101,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   *safety_out = cur.safety;
   *drop_out = cur.drop;
   *ctas_out = cur.ctas;
+  *slack_out = cur.slack;
   *best_ms = best;
   return INCA_OK;
 }

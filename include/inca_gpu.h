@@ -156,7 +156,10 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
  * estimates, the share of the tolerance given to left-out (quartet, tile) pairs
  * (drop_fraction, below 0.5; < 0: the default 0.05), and the register budget of the one-pass
  * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20, one compiled
- * instantiation each; 0: the default 16). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
+ * instantiation each; 0: the default 16), and the slack of the cheap tier (cheap_slack, 0..30:
+ * a (quartet, tile) pair is evaluated in plain FP32 when its rigorous error bound is at most
+ * 2^cheap_slack times the tile's drop threshold; that bound joins the left-out mass, which is
+ * checked after the pass as before, so a large slack can cost a repeat, never accuracy). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
  * (median of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
  * context and reports it with the time of the default schedule; the last evaluation's results
  * stay on the device. inca_set_tuning sets a schedule (NULL: the defaults). Every schedule meets
@@ -169,6 +172,7 @@ typedef struct inca_tuning {
   double default_ms;  /* output of inca_autotune */
   double drop_fraction;
   int32_t ctas_per_sm;
+  int32_t cheap_slack;
 } inca_tuning;
 int inca_autotune(inca_ctx* ctx, double tol, int32_t reps, inca_tuning* chosen);
 int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);

@@ -77,20 +77,23 @@ def test_estimate_pass_items(ctx, scan_fp64, monkeypatch, items):
     np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
 
 
-@pytest.mark.parametrize("cheap,drop", [("1", "0.4"), ("1", "0.05"), ("0", "0.05")])
-def test_cheap_tier(ctx, scan_fp64, monkeypatch, cheap, drop):
-    # pairs whose rigorous FP32 error bound fits under the drop threshold take the cheap tier
-    # (plain FP32, hardware ex2); the tolerance holds with and without it, and with a large
-    # share of the tolerance given to left-out and cheap pairs
+@pytest.mark.parametrize("cheap,drop,slack", [("1", "0.4", "0"), ("1", "0.05", "0"), ("0", "0.05", "0"),
+                                              ("1", "0.2", "6"), ("1", "0.2", "30")])
+def test_cheap_tier(ctx, scan_fp64, monkeypatch, cheap, drop, slack):
+    # pairs whose rigorous FP32 error bound fits under the drop threshold (times 2^slack) take
+    # the cheap tier (plain FP32, hardware ex2); the tolerance holds with and without it, with a
+    # large share of the tolerance given to left-out and cheap pairs, and with a slack so large
+    # that the left-out mass exceeds its check and the pass is repeated without leaving out
     monkeypatch.setenv("INCA_CHEAP_TIER", cheap)
     monkeypatch.setenv("INCA_DROP_FRACTION", drop)
+    monkeypatch.setenv("INCA_CHEAP_SLACK", slack)
     I = _scan_mixed(ctx)
     rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
     assert rel.max() <= 1e-8, rel.max()
     st = ctx.stats()
-    if cheap == "1":
+    if cheap == "1" and slack != "30":
         assert st["cheap_pairs"] > 0
-    else:
+    else:  # off, or repeated without leaving anything out
         assert st["cheap_pairs"] == 0
     eager = ctx.eval(mode=1, tol=1e-8)
     np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
@@ -170,14 +173,16 @@ def test_autotune_keeps_tolerance(ctx, scan_fp64):
     assert t["estimate_safety"] in (0.3, 0.5, 0.7)
     assert t["drop_fraction"] in (0.02, 0.05, 0.1, 0.2)
     assert t["ctas_per_sm"] in (12, 16, 20)
+    assert t["cheap_slack"] in (0, 2, 4, 6, 8)
     assert 0 < t["best_ms"] <= t["default_ms"]
     try:
         # the tuned schedule stays in the context; every schedule meets the tolerance
         I = _scan_mixed(ctx)
         rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
         assert rel.max() <= 1e-8, rel.max()
-        for ipc, stride, safety, drop, ctas in ((4, 32, 0.3, 0.2, 12), (48, 8, 0.7, 0.02, 20), (12, 16, 0.5, 0.05, 16)):
-            ctx.set_tuning(ipc, stride, safety, drop, ctas)
+        for ipc, stride, safety, drop, ctas, slack in ((4, 32, 0.3, 0.2, 12, 8), (48, 8, 0.7, 0.02, 20, 0),
+                                                      (12, 16, 0.5, 0.05, 16, 30)):
+            ctx.set_tuning(ipc, stride, safety, drop, ctas, slack)
             I = _scan_mixed(ctx)
             rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
             assert rel.max() <= 1e-8, (ipc, stride, safety, rel.max())
