@@ -170,7 +170,8 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_full, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CH4 closed-shell DM2)",
             "config": {"workload": "ch4_radial_scan_590", "points": 62390, "quartets": int(len(v)),
-                       "cpu_sample": sample,
+                       "cpu_sample": sample, "step_rates": rates,
+                       "step_rate_rel_std": (statistics.pstdev(rates) / val) if len(rates) > 1 else 0.0,
                        "ms_per_step_basis": "the full scan (all surviving quartets at all points) at the "
                                             "sampled rate"},
             "cpu_baseline": {"value": val, "unit": "quartet-points/s", "cores": cores, "kind": "port",
