@@ -446,17 +446,6 @@ __device__ __forceinline__ void term_df_n(const float* const (&R)[N], const int 
   for (int n = 0; n < N; ++n) out[n] = df_mul(t[n], f2{R[n][8], R[n][9]});
 }
 
-// The double-float term of record R at one point (compact code for the correction pass).
-__device__ __noinline__ f2 term_df(const float* __restrict__ R, int L0, int L1, int L2, float rx, float ry, float rz,
-                                   float lx, float ly, float lz, const float2* __restrict__ tab) {
-  const int L[3] = {L0, L1, L2};
-  const float rh[1][3] = {{rx, ry, rz}}, rl[1][3] = {{lx, ly, lz}};
-  const float* const Rs[1] = {R};
-  f2 out[1];
-  term_df_n<1>(Rs, L, rh, rl, tab, out);
-  return out[0];
-}
-
 struct f2x2 {
   f2 a, b;
 };
@@ -485,6 +474,62 @@ __device__ __forceinline__ void load_points(const float4* __restrict__ phi, cons
     }
     rh[0][p] = h.x; rh[1][p] = h.y; rh[2][p] = h.z;
     rl[0][p] = l.x; rl[1][p] = l.y; rl[2][p] = l.z;
+  }
+}
+
+// The noted corrections of one chunk (nm[p]: records q whose term at the lane's point p is to be
+// evaluated in double-float), two terms per lane and round, taken in (point, record) order from
+// all the lane's points; each lane adds its results to its points' double-float sums corr_s.
+// Every lane takes part in every round (lanes without a term left skip the work), so the
+// class-uniform record data in shared memory serves the whole warp.
+__device__ __forceinline__ void correction_rounds(uint32_t (&nm)[kPPT], const float* __restrict__ st, int rs,
+                                                  const int L[3], const TileInfo& T, int lane,
+                                                  const float4* __restrict__ phi, const float4* __restrict__ plo,
+                                                  const float2* __restrict__ tab, float2 (*corr_s)[32],
+                                                  unsigned long long& nround, unsigned long long& ncorr) {
+  uint32_t any_left = 0u;
+#pragma unroll
+  for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
+  while (__any_sync(0xffffffffu, any_left != 0u)) {
+    ++nround;
+    int pa = -1, qa = 0, pb = -1, qb = 0;
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p)
+      if (pa < 0 && nm[p]) {
+        pa = p;
+        qa = __ffs(nm[p]) - 1;
+        nm[p] &= nm[p] - 1;
+      }
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p)
+      if (pb < 0 && nm[p]) {
+        pb = p;
+        qb = __ffs(nm[p]) - 1;
+        nm[p] &= nm[p] - 1;
+      }
+    any_left = 0u;
+#pragma unroll
+    for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
+    if (pa >= 0) {
+      const bool two = pb >= 0;
+      if (!two) {  // a lone term is paired with itself and the copy discarded
+        pb = pa;
+        qb = qa;
+      }
+      const int64_t ga = T.start + lane + 32 * pa, gb = T.start + lane + 32 * pb;
+      const f2x2 r = term_df2p(st + qa * rs, st + qb * rs, L[0], L[1], L[2], phi[ga], plo[ga], phi[gb], plo[gb],
+                               tab);
+      float2 ca = corr_s[pa][lane];
+      f2 c = df_add(f2{ca.x, ca.y}, r.a);
+      if (two && pb == pa) c = df_add(c, r.b);
+      corr_s[pa][lane] = make_float2(c.hi, c.lo);
+      if (two && pb != pa) {
+        const float2 cb = corr_s[pb][lane];
+        const f2 d = df_add(f2{cb.x, cb.y}, r.b);
+        corr_s[pb][lane] = make_float2(d.hi, d.lo);
+      }
+      ncorr += two ? 2 : 1;
+    }
   }
 }
 
@@ -644,8 +689,12 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
           if (kFuse && e[p] > tau[p]) {
+            // corrected in double-float below: it carries no FP32 error, so neither its value
+            // nor its error bound enters the sums (the exact thresholds then rest on the
+            // uncorrected terms alone, which is all the variance bound needs)
             nm[p] |= 1u << q;
             t[p] = 0.0f;
+            e[p] = 0.0f;
           }
           if (kEst) {
             sh[p] = __fadd_rn(sh[p], t[p]);
@@ -658,51 +707,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         }
       }
       if (kFuse) {
-        // two terms per lane and round, taken in (point, record) order from all the lane's points
-        uint32_t any_left = 0u;
-#pragma unroll
-        for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
-        while (__any_sync(0xffffffffu, any_left != 0u)) {
-          ++nround;
-          int pa = -1, qa = 0, pb = -1, qb = 0;
-#pragma unroll
-          for (int p = 0; p < kPPT; ++p)
-            if (pa < 0 && nm[p]) {
-              pa = p;
-              qa = __ffs(nm[p]) - 1;
-              nm[p] &= nm[p] - 1;
-            }
-#pragma unroll
-          for (int p = 0; p < kPPT; ++p)
-            if (pb < 0 && nm[p]) {
-              pb = p;
-              qb = __ffs(nm[p]) - 1;
-              nm[p] &= nm[p] - 1;
-            }
-          any_left = 0u;
-#pragma unroll
-          for (int p = 0; p < kPPT; ++p) any_left |= nm[p];
-          if (pa >= 0) {
-            const bool two = pb >= 0;
-            if (!two) {  // a lone term is paired with itself and the copy discarded
-              pb = pa;
-              qb = qa;
-            }
-            const int64_t ga = T.start + lane + 32 * pa, gb = T.start + lane + 32 * pb;
-            const f2x2 r = term_df2p(st + qa * rs, st + qb * rs, L[0], L[1], L[2], phi[ga],
-                                     plo[ga], phi[gb], plo[gb], tab);
-            float2 ca = corr_s[pa][lane];
-            f2 c = df_add(f2{ca.x, ca.y}, r.a);
-            if (two && pb == pa) c = df_add(c, r.b);
-            corr_s[pa][lane] = make_float2(c.hi, c.lo);
-            if (two && pb != pa) {
-              const float2 cb = corr_s[pb][lane];
-              const f2 d = df_add(f2{cb.x, cb.y}, r.b);
-              corr_s[pb][lane] = make_float2(d.hi, d.lo);
-            }
-            ncorr += two ? 2 : 1;
-          }
-        }
+        correction_rounds(nm, st, rs, L, T, lane, phi, plo, tab, corr_s, nround, ncorr);
       }
       // renormalise the FP32 pair every chunk; move it to FP64 every kFold chunks (the plain
       // sums of the estimate pass after every chunk)
@@ -919,10 +924,11 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
   extern __shared__ __align__(128) unsigned char dsm[];
   const Stage S = stage_view(dsm, stage_floats);
   __shared__ float2 tab[kExpTab + 1];
+  __shared__ float2 corr_s[kPPT][32];
   const int lane = threadIdx.x;
   for (int i = lane; i <= kExpTab; i += 32) tab[i] = exp_tab[i];
   stage_init(S);
-  unsigned long long n32 = 0, ndf = 0, npts = 0;
+  unsigned long long n32 = 0, ndf = 0, npts = 0, nround = 0;
   int k = 0;
   for (;;) {
     const int64_t item = next_item(work);
@@ -960,11 +966,10 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     for (int b = 0; b < 6; ++b) wbox[b] = wtbox[wtile * 8 + b];
     const float thr = lt_drop ? fmaxf(kSkipLog2, lt_drop[wtile]) : kSkipLog2;
     double acc[kPPT];
-    f2 corr[kPPT];
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
       acc[p] = 0.0;
-      corr[p] = {0.0f, 0.0f};
+      corr_s[p][lane] = make_float2(0.0f, 0.0f);
     }
     __syncwarp();
     int nfold = 0;
@@ -975,7 +980,8 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
       const WorkChunk w = chunks[ch];
       const ClassSeg sg = segs[w.cls];
       const float* st = S.buf(k);
-      const int L[3] = {sg.L[0], sg.L[1], sg.L[2]};
+      const int L[3] = {__reduce_max_sync(0xffffffffu, sg.L[0]), __reduce_max_sync(0xffffffffu, sg.L[1]),
+                        __reduce_max_sync(0xffffffffu, sg.L[2])};
       const float* Rq = st + lane * sg.stride32;
       // the skip decision of the pass over all terms (same box, arithmetic and threshold)
       const float lb = lane < w.count ? log2_bound(Rq, L, wbox) : -HUGE_VALF;
@@ -998,34 +1004,41 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
         ndf += __popc(any);
         n32 += __popc(live & ~any);
       }
+      // the terms to correct: above the exact threshold and not corrected by the one-pass kernel
+      // (which corrected the live terms above the estimated one); the FP32 value a live term
+      // put into the pass's sum comes off here, its double-float value goes on in the rounds
+      uint32_t nm[kPPT];
 #pragma unroll
       for (int p = 0; p < kPPT; ++p) {
+        nm[p] = 0u;
         uint32_t m = msub[p];
+        float2 c = corr_s[p][lane];
+        f2 cp{c.x, c.y};
         while (m) {
           const int q = __ffs(m) - 1;
           m &= m - 1;
           const float* R = st + q * sg.stride32;
           float t32 = 0.0f, e32 = 0.0f;
           term32_one(R, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], &t32, &e32);
-          // with pt_tau_est: the one-pass kernel already corrected the live terms above it
           const bool live_q = (live >> q) & 1u;
           const bool need = e32 > tau[p] && !(live_q && e32 > tau_est[p]);
-          if (__any_sync(0xffffffffu, need)) {
-            if (lane == 0) ++npts;
-            if (need) {
-              f2 tdf = term_df(R, L[0], L[1], L[2], rh[0][p], rh[1][p], rh[2][p], rl[0][p], rl[1][p], rl[2][p], tab);
-              if (live_q) tdf = df_add(tdf, f2{-t32, 0.0f});
-              corr[p] = df_add(corr[p], tdf);
-            }
+          if (need) {
+            nm[p] |= 1u << q;
+            if (live_q) cp = df_add(cp, f2{-t32, 0.0f});
           }
         }
+        corr_s[p][lane] = make_float2(cp.hi, cp.lo);
       }
+      unsigned long long ncorr = 0;
+      correction_rounds(nm, st, sg.stride32, L, T, lane, phi, plo, tab, corr_s, nround, ncorr);
+      npts += ncorr;
       if (++nfold == kFold) {
         nfold = 0;
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
-          acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
-          corr[p] = {0.0f, 0.0f};
+          const float2 c = corr_s[p][lane];
+          acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
+          corr_s[p][lane] = make_float2(0.0f, 0.0f);
         }
       }
       __syncwarp();
@@ -1036,14 +1049,16 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
     }
 #pragma unroll
     for (int p = 0; p < kPPT; ++p) {
-      acc[p] += static_cast<double>(corr[p].hi) + static_cast<double>(corr[p].lo);
+      const float2 c = corr_s[p][lane];
+      acc[p] += static_cast<double>(c.x) + static_cast<double>(c.y);
       const int j = lane + 32 * p;
       if (j < T.count) part[pat + T.start + j] = acc[p];
     }
   }
+  for (int o = 16; o > 0; o >>= 1) npts += __shfl_xor_sync(0xffffffffu, npts, o);
   if (lane == 0) {
     atomicAdd(&stats[0], n32);
-    atomicAdd(&stats[1], ndf);
+    atomicAdd(&stats[1], ndf + nround);
     atomicAdd(&stats[3], npts);
   }
 }
@@ -1942,14 +1957,14 @@ int mixed_finish(inca_ctx* c, const MixedPlan& P, Events* ev, bool* retry) {
     c->pairs_fp32 = static_cast<int64_t>(hs[0]);
     c->pairs_fp64 = static_cast<int64_t>(hs[1]) + static_cast<int64_t>(hs[5]);
     c->pairs_skip = static_cast<int64_t>(hs[2]);
-    c->corrected_points = static_cast<int64_t>(hs[3]) + 32 * static_cast<int64_t>(hs[7]);
+    c->corrected_points = static_cast<int64_t>(hs[3]) + static_cast<int64_t>(hs[7]);
     c->pairs_cheap = static_cast<int64_t>(hs[13]);
   } else {
     c->pairs_cheap = 0;
     c->pairs_fp32 = static_cast<int64_t>(hs[4]);
     c->pairs_fp64 = static_cast<int64_t>(hs[5]);
     c->pairs_skip = static_cast<int64_t>(hs[2]);
-    c->corrected_points = static_cast<int64_t>(hs[7]) * 32;
+    c->corrected_points = static_cast<int64_t>(hs[7]);
   }
   return INCA_OK;
 }
@@ -2074,7 +2089,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   *default_ms = best;
   const int ipcs[] = {4, 8, 12, 24, 48};
   const int strides[] = {8, 16, 32, 64};
-  const double safeties[] = {0.3, 0.5, 0.7};
+  const double safeties[] = {0.3, 0.5, 0.7, 1.0, 1.25};
   const double drops[] = {0.02, 0.05, 0.1, 0.2};
   const int ctass[] = {12, 16, 20};
   const int slacks[] = {0, 2, 4, 6, 8};
