@@ -2090,7 +2090,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   const int ipcs[] = {4, 8, 12, 24, 48};
   const int strides[] = {8, 16, 32, 64};
   const double safeties[] = {0.3, 0.5, 0.7, 1.0, 1.25};
-  const double drops[] = {0.02, 0.05, 0.1, 0.2};
+  const double drops[] = {0.02, 0.05, 0.1, 0.2, 0.3};
   const int ctass[] = {12, 16, 20};
   const int slacks[] = {0, 2, 4, 6, 8};
   auto consider = [&](Sched s) -> int {
