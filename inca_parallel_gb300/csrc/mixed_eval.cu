@@ -71,11 +71,12 @@ constexpr double kTestScale = 1.0 / 1.01;  // correct when e > tau / 1.01
 // a usable estimate, and the exact thresholds and the band pass keep the tolerance regardless)
 constexpr int64_t kFuseMinPoints = 2048;
 constexpr int64_t kSampleStride = 16;
-constexpr double kEstSafety = 0.5;
+constexpr double kEstSafety = 0.7;
 constexpr double kCubeMargin = 2.0;
 // Share of the tolerance given to terms left out of the one-pass form (their bounds over the
 // tile sum to at most this share of eps |O|, checked after the pass).
-constexpr double kDropFrac = 0.05;
+constexpr double kDropFrac = 0.1;
+constexpr int kCheapSlack = 4;           // default slack of the cheap tier (powers of two)
 constexpr float kSkipLog2 = -120.0f;     // pass-1 skip: bound below 2^-120
 constexpr int kFold = 8;                 // chunks between FP64 folds
 constexpr int kItemsPerCta = 12;         // persistent passes: work items per resident CTA
@@ -1677,7 +1678,8 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   // threshold (0: within the threshold, so the left-out mass keeps its a-priori bound; larger:
   // checked after the pass like the rest of the left-out mass). Passed to the kernels as
   // 0 (off) or 1 + slack.
-  const int slack = static_cast<int>(env_knob("INCA_CHEAP_SLACK", c->tune_cheap_slack >= 0 ? c->tune_cheap_slack : 0,
+  const int slack = static_cast<int>(env_knob("INCA_CHEAP_SLACK", c->tune_cheap_slack >= 0 ? c->tune_cheap_slack
+                                                                                           : kCheapSlack,
                                               0.0, 31.0));
   P.cheap = env_knob("INCA_CHEAP_TIER", 1.0, 0.0, 2.0) >= 0.5 ? 1 + slack : 0;
   // test of the bounded staging waits: the pass-1 kernels start no copy and give up waiting
@@ -2082,7 +2084,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     *ms = t[t.size() / 2];
     return INCA_OK;
   };
-  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, 0};
+  Sched cur{kItemsPerCta, static_cast<int>(kSampleStride), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, kCheapSlack};
   double best = 0.0;
   int st = timed(cur, &best);
   if (st) return st;

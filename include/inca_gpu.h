@@ -154,7 +154,7 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
 /* Schedule of the mixed evaluation: work items per resident CTA of the persistent passes,
  * the stride of the grid sample that estimates the thresholds, the factor applied to the
  * estimates, the share of the tolerance given to left-out (quartet, tile) pairs
- * (drop_fraction, below 0.5; < 0: the default 0.05), and the register budget of the one-pass
+ * (drop_fraction, below 0.5; < 0: the default 0.1), and the register budget of the one-pass
  * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20, one compiled
  * instantiation each; 0: the default 16), and the slack of the cheap tier (cheap_slack, 0..30:
  * a (quartet, tile) pair is evaluated in plain FP32 when its rigorous error bound is at most
