@@ -254,7 +254,10 @@ __device__ __forceinline__ void terms32(const float* __restrict__ R, const int L
 // the hardware ex2.approx, the FP32 coefficients and an FP32 sum over the chunk. Instead of
 // entering the statistical error model, each such term carries a rigorous bound of its error,
 // c 2^lb (2^lb bounds |term| over the tile), which is added to the tile's left-out bound mass
-// like a dropped term's 2^lb: the pair qualifies when c 2^lb is at most the drop threshold.
+// like a dropped term's 2^lb: the pair qualifies when c 2^lb is at most 2^slack times the drop
+// threshold (slack 0 keeps the a-priori bound of the left-out mass; with a larger slack the
+// check after the pass -- repeat without leaving out if the mass took more than half the
+// budget -- guards the tolerance).
 //
 // The bound, with u = 2^-24, K_d = 2 s X_d + |b_d| (X_d: largest |x_d| over the tile box) and
 // m_d / M_d the smallest / largest |u_d| over the box (as in log2_bound):
