@@ -150,3 +150,18 @@ def test_batch_graph_replay_bit_identical(ctx, molecules):
     for _ in range(3):
         np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
         np.testing.assert_array_equal(ctx.radial_plot()[1], per_mol)
+
+
+def test_batch_fp64_screened(ctx, molecules):
+    # the screened FP64 form on a batch: the one-pass plan over all molecules, FP64 terms, the
+    # same pairs left out as the mixed form; within half the tolerance of the plain FP64 form
+    from inca_parallel_gb300 import INCA_FP64_SCREENED
+    ctx.batch_clear()
+    for b, D in molecules:
+        ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *SCAN)
+    ctx.batch_prepare(THRESH)
+    ref = ctx.batch_eval(mode=0)
+    got = ctx.batch_eval(mode=INCA_FP64_SCREENED, tol=1e-8)
+    for r, g in zip(ref, got):
+        assert np.max(np.abs(g - r) / np.abs(r)) <= 0.5e-8
+    assert ctx.stats()["skipped_pairs"] > 0

@@ -118,3 +118,14 @@ def test_d_shells(exact):
         assert not np.isnan(Is).any()
         scale = np.abs(I64).max()
         assert np.abs(Is - I64).max() <= 1e-12 * scale
+
+
+def test_fp64_screened_on_a_lattice_is_the_fp64_form(ch4):
+    # cube lattices have no drop thresholds of the one-pass form: the screened mode runs as FP64
+    from inca_parallel_gb300 import INCA_FP64_SCREENED, Context
+    with Context(0) as ctx:
+        ctx.set_primitives(ch4["alpha"], ch4["tmn"], ch4["xyz"])
+        ctx.set_quartets(ch4["ijkl"], ch4["v"])
+        ctx.prepare(1e-12)
+        ctx.grid_cube([0, 0, 0], [0.2, 0.2, 0.2], [10, 10, 10])
+        np.testing.assert_array_equal(ctx.eval(mode=INCA_FP64_SCREENED, tol=1e-8), ctx.eval(mode=0))
