@@ -433,7 +433,7 @@ def gpu_arm(args):
     # bind(C) shim), tuned schedule;
     # the quartet input and the I(r) output live in pinned host memory
     ctx.set_tuning(sched["items_per_cta"], sched["sample_stride"], sched["estimate_safety"], sched["drop_fraction"],
-                   sched["ctas_per_sm"], sched["cheap_slack"])
+                   sched["ctas_per_sm"], sched["cheap_slack"], sched["points_per_lane"])
     ctx.grid_scan(*scan_args)
     pin_ijkl = torch.empty(ijkl.size, dtype=torch.int32, pin_memory=True).numpy()
     pin_v = torch.empty(v.size, dtype=torch.float64, pin_memory=True).numpy()
@@ -527,6 +527,7 @@ def gpu_arm(args):
                                     "estimate_safety": sched["estimate_safety"],
                                     "drop_fraction": sched["drop_fraction"], "ctas_per_sm": sched["ctas_per_sm"],
                                     "cheap_slack": sched["cheap_slack"],
+                                    "points_per_lane": sched["points_per_lane"],
                                     "default_ms": sched["default_ms"],
                                     "tuned_ms": sched["best_ms"], "tuning_s": t_tune},
                        "radial_integral_nrad50_nang110": {"fp64_ms": ri["fp64"]["ms"], "mixed_ms": ri["mixed"]["ms"],
@@ -534,7 +535,8 @@ def gpu_arm(args):
                                                           "tolerance": TOL_INTEGRAL,
                                                           "schedule": {k: ri_sched[k] for k in (
                                                               "items_per_cta", "sample_stride", "estimate_safety",
-                                                              "drop_fraction", "ctas_per_sm", "cheap_slack")}},
+                                                              "drop_fraction", "ctas_per_sm", "cheap_slack",
+                                                              "points_per_lane")}},
                        "fp64_screened_form": {"ms_per_step": ms64s, "value": qp / (ms64s * 1e-3),
                                               "max_rel_err_I_s_vs_fp64": rel_scan64s,
                                               "pairs_evaluated": stats64s["precise_pairs"],

@@ -30,7 +30,8 @@ VP = ctypes.c_void_p
 class Tuning(ctypes.Structure):
     _fields_ = [("items_per_cta", ctypes.c_int32), ("sample_stride", ctypes.c_int32),
                 ("estimate_safety", ctypes.c_double), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double),
-                ("drop_fraction", ctypes.c_double), ("ctas_per_sm", ctypes.c_int32), ("cheap_slack", ctypes.c_int32)]
+                ("drop_fraction", ctypes.c_double), ("ctas_per_sm", ctypes.c_int32), ("cheap_slack", ctypes.c_int32),
+                ("points_per_lane", ctypes.c_int32)]
 
 
 class Counts(ctypes.Structure):
@@ -322,11 +323,12 @@ class Context:
         return {f: getattr(t, f) for f, _ in Tuning._fields_}
 
     def set_tuning(self, items_per_cta=None, sample_stride=None, estimate_safety=None, drop_fraction=-1.0,
-                   ctas_per_sm=0, cheap_slack=0):
+                   ctas_per_sm=0, cheap_slack=0, points_per_lane=0):
         if items_per_cta is None:
             self._check(self.lib.inca_set_tuning(self.h, None))
             return
-        t = Tuning(items_per_cta, sample_stride, estimate_safety, 0.0, 0.0, drop_fraction, ctas_per_sm, cheap_slack)
+        t = Tuning(items_per_cta, sample_stride, estimate_safety, 0.0, 0.0, drop_fraction, ctas_per_sm, cheap_slack,
+                   points_per_lane)
         self._check(self.lib.inca_set_tuning(self.h, ctypes.byref(t)))
 
     def eval_graph(self, mode=INCA_MIXED, tol=1e-10, copy=True):

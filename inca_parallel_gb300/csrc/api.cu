@@ -398,10 +398,10 @@ int inca_autotune(inca_ctx* c, double tol, int32_t reps, inca_tuning* chosen) {
   if (!c->prepared) return set_error(c, INCA_E_STATE, "inca_autotune: call inca_prepare first");
   if (c->grid_kind == GRID_NONE || c->ngrid <= 0) return set_error(c, INCA_E_STATE, "inca_autotune: no grid");
   if (c->d_ivec.reserve(c->ngrid)) return set_error(c, INCA_E_NOMEM, "ivec");
-  int ipc = 0, stride = 0, ctas = 0, slack = 0;
+  int ipc = 0, stride = 0, ctas = 0, slack = 0, ppt = 0;
   double safety = 0, drop = 0, best = 0, dflt = 0;
   const int st = autotune_mixed(c, tol > 0 ? tol : 1e-10, std::max(1, reps), &ipc, &stride, &safety, &drop, &ctas,
-                                &slack, &best, &dflt);
+                                &slack, &ppt, &best, &dflt);
   if (st) return st;
   c->evaluated = true;
   if (chosen) {
@@ -411,6 +411,7 @@ int inca_autotune(inca_ctx* c, double tol, int32_t reps, inca_tuning* chosen) {
     chosen->drop_fraction = drop;
     chosen->ctas_per_sm = ctas;
     chosen->cheap_slack = slack;
+    chosen->points_per_lane = ppt;
     chosen->best_ms = best;
     chosen->default_ms = dflt;
   }
@@ -421,7 +422,8 @@ int inca_set_tuning(inca_ctx* c, const inca_tuning* t) {
   CTX_CHECK(c);
   if (t && (t->items_per_cta < 1 || t->items_per_cta > 1024 || t->sample_stride < 1 || t->sample_stride > 1024 ||
             !(t->estimate_safety >= 0.0) || !(t->drop_fraction < 0.5) ||
-            !(t->ctas_per_sm == 0 || t->ctas_per_sm == 12 || t->ctas_per_sm == 16 || t->ctas_per_sm == 20) ||
+            !valid_pass_shape(t->points_per_lane ? t->points_per_lane : 4,
+                              t->ctas_per_sm ? t->ctas_per_sm : 16) ||
             t->cheap_slack < 0 || t->cheap_slack > 30))
     return set_error(c, INCA_E_ARG, "inca_set_tuning: bad values");
   c->tune_items_per_cta = t ? t->items_per_cta : 0;
@@ -430,6 +432,7 @@ int inca_set_tuning(inca_ctx* c, const inca_tuning* t) {
   c->tune_drop = t ? t->drop_fraction : -1.0;
   c->tune_ctas = t ? t->ctas_per_sm : 0;
   c->tune_cheap_slack = t ? t->cheap_slack : -1;
+  c->tune_ppt = t ? t->points_per_lane : 0;
   return INCA_OK;
 }
 

@@ -197,9 +197,10 @@ struct inca_ctx {
 
   // mixed evaluation: Morton-sorted copy of the grid (rebuilt when the grid changes)
   int64_t mix_version = -1;
+  int mix_ppt = 4;                    // points per lane of its warp tiles (a tile: 32 x mix_ppt)
   inca::DevBuf<float4> d_phi, d_plo;  // FP32 hi / lo parts of the sorted points
   inca::DevBuf<int64_t> d_perm;       // sorted position -> grid index
-  inca::DevBuf<float> d_wtbox;        // per 128-point warp tile: lo[3], hi[3], 2 pad
+  inca::DevBuf<float> d_wtbox;        // per warp tile: lo[3], hi[3], 2 pad
   inca::DevBuf<inca::TileInfo> d_tiles;  // tiles of the sorted grid
   int64_t ntiles = 0;
   std::vector<inca::MolSpan> mol_span;   // per molecule: its tiles and sorted points
@@ -236,6 +237,7 @@ struct inca_ctx {
   double tune_safety = -1.0;
   double tune_drop = -1.0;
   int tune_ctas = 0;  // resident CTAs per SM of the one-pass kernel (0: the default)
+  int tune_ppt = 0;   // points per lane of its warp tiles (0: the default, 4)
   int tune_cheap_slack = -1;  // cheap-tier slack in powers of two (-1: the default, 0)
   int sample_stride_built = 0;  // stride of the current sorted sample
 
@@ -265,7 +267,8 @@ int gen_closed_shell_into(inca_ctx* c, int n, const double* D, int unique, int b
 int eval_device(inca_ctx* c, int mode, double tol, bool graph = false);
 // mixed_eval.cu
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc, int* stride, double* safety, double* drop,
-                   int* ctas, int* slack, double* best_ms, double* default_ms);
+                   int* ctas, int* slack, int* ppt, double* best_ms, double* default_ms);
+bool valid_pass_shape(int ppt, int ctas);
 int ensure_exp_table(inca_ctx* c);
 // cube_eval.cu
 bool cube_separable(const inca_ctx* c);

@@ -10,8 +10,8 @@
 // double-float arithmetic (~2^-44) and the difference is added.
 //
 // Work layout. Points are evaluated in Morton order (a sorted copy of the grid). A CTA is one
-// warp owning 128 consecutive points (4 per lane, 32-point sub-tiles p = lane + 32 k), each a
-// compact region with a bounding box. The CTA walks a strided subset of the class-uniform
+// warp owning a tile of 32 kPPT consecutive points (kPPT = 3, 4 or 5 per lane, set by the
+// schedule; 32-point sub-tiles p = lane + 32 k), each a compact region with a bounding box. The CTA walks a strided subset of the class-uniform
 // chunks (<= 32 quartet records of one angular class); each chunk is staged into shared memory
 // by a 1-D TMA bulk copy (cp.async.bulk + mbarrier), double-buffered so the next chunk's copy
 // overlaps the current chunk's arithmetic. All waits are bounded; a wait that gives up sets an
@@ -50,11 +50,11 @@ int choose_splits(int64_t tiles, int64_t nchunks, int num_sms, int ctas_per_sm);
 
 namespace {
 
-#ifndef INCA_PPT
-#define INCA_PPT 4
-#endif
-constexpr int kPPT = INCA_PPT;          // points per lane
-constexpr int kWarpTile = 32 * kPPT;    // 128 points per CTA (one warp)
+// Points per lane (kPPT, a template parameter of the kernels): a one-warp CTA owns a tile of
+// 32 kPPT consecutive sorted points, as kPPT sub-tiles of 32 (points lane + 32 p). The schedule
+// picks 3, 4 or 5; the grid sample behind the threshold estimates always uses 4.
+constexpr int kDefaultPPT = 4;
+constexpr int kSamplePPT = 4;
 constexpr int kMaxStride32 = (12 + 2 * 3 * kMaxCoef + 3) & ~3;
 // tau = kTauScale (eps |O|)^2 / E_O: the error of an uncorrected term is a sum of independent
 // round-to-nearest errors bounded in total by e_t, so its variance is <= e_t^2 / 3, and
@@ -465,6 +465,7 @@ __device__ __noinline__ f2x2 term_df2p(const float* __restrict__ Ra, const float
   return {out[0], out[1]};
 }
 
+template <int kPPT>
 __device__ __forceinline__ void load_points(const float4* __restrict__ phi, const float4* __restrict__ plo,
                                             const TileInfo& T, int lane, float (&rh)[3][kPPT],
                                             float (&rl)[3][kPPT]) {
@@ -486,6 +487,7 @@ __device__ __forceinline__ void load_points(const float4* __restrict__ phi, cons
 // all the lane's points; each lane adds its results to its points' double-float sums corr_s.
 // Every lane takes part in every round (lanes without a term left skip the work), so the
 // class-uniform record data in shared memory serves the whole warp.
+template <int kPPT>
 __device__ __forceinline__ void correction_rounds(uint32_t (&nm)[kPPT], const float* __restrict__ st, int rs,
                                                   const int L[3], const TileInfo& T, int lane,
                                                   const float4* __restrict__ phi, const float4* __restrict__ plo,
@@ -548,7 +550,8 @@ __device__ __forceinline__ void correction_rounds(uint32_t (&nm)[kPPT], const fl
 //   Its sums only set the estimated thresholds (an estimate that is off costs corrections or a
 //   band pass, never accuracy), so its terms skip the compensation of u (kComp = false) and are
 //   summed in plain FP32, moved to FP64 after every chunk; the error bounds are the same.
-template <bool kFuse, bool kEst = false, int kCtas = INCA_PASS_CTAS_PER_SM, bool kWaitTest = false>
+template <bool kFuse, bool kEst = false, int kCtas = INCA_PASS_CTAS_PER_SM, bool kWaitTest = false,
+          int kPPT = kDefaultPPT>
 __global__ void __launch_bounds__(32, kCtas)
 k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
@@ -779,6 +782,7 @@ k_pass1(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
 // every remaining term in FP64 (the hi + lo pairs of the FP32 records carry each value to about
 // 2^-48), without error bounds or corrections. It prices the precision alone: the mixed form
 // against this kernel differs only in the arithmetic of the terms it evaluates.
+template <int kPPT>
 __device__ __forceinline__ void term_f64(const float* __restrict__ R, const int L[3], const double (&x)[3][kPPT],
                                          double (&acc)[kPPT]) {
   const double s = static_cast<double>(R[0]) + static_cast<double>(R[1]);
@@ -819,6 +823,7 @@ __device__ __forceinline__ void term_f64(const float* __restrict__ R, const int 
   for (int p = 0; p < kPPT; ++p) acc[p] += t[p];
 }
 
+template <int kPPT>
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass_f64(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
            const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
@@ -917,6 +922,7 @@ k_pass_f64(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw,
 }
 
 // ---------------------------------------------------------------- pass 2 (corrections)
+template <int kPPT>
 __global__ void __launch_bounds__(32, INCA_PASS_CTAS_PER_SM)
 k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, int nmol,
         const ClassSeg* __restrict__ segs, const float* __restrict__ rec32, const float4* __restrict__ phi,
@@ -1146,8 +1152,9 @@ __global__ void __launch_bounds__(1024) k_bbox(int64_t n, const double* __restri
   if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
 }
 
-// Bounding boxes (FP32, rounded outwards) of each 128-point tile and its four 32-point
+// Bounding boxes (FP32, rounded outwards) of each tile of 32 kPPT points and its kPPT 32-point
 // sub-tiles (points lane + 32 p). One warp per tile.
+template <int kPPT>
 __global__ void k_boxes(const TileInfo* __restrict__ tiles, int64_t nwt, const float4* __restrict__ phi,
                         const float4* __restrict__ plo, float* wbox, float* gbox) {
   const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
@@ -1189,6 +1196,7 @@ __global__ void k_boxes(const TileInfo* __restrict__ tiles, int64_t nwt, const f
 // A term is corrected when its error bound e exceeds tau_g / 1.01 (the stored value).
 // mode 0: tau = T_seg / w_g; mode 1 (max-norm): tau = T / E_g; mode 2: per point;
 // mode 3: tau = T (uniform).
+template <int kPPT>
 __global__ void k_thresholds(const TileInfo* __restrict__ tiles, int64_t ngroups, int mode,
                              const int64_t* __restrict__ perm, const int* __restrict__ seg_of,
                              const double* __restrict__ segT, const double* __restrict__ w,
@@ -1228,6 +1236,7 @@ __global__ void k_thresholds(const TileInfo* __restrict__ tiles, int64_t ngroups
 
 // Sub-tiles where the exact threshold fell below the estimate used by the one-pass kernel:
 // g_lt = log2 of the smallest exact threshold among those points (else +inf); counts them.
+template <int kPPT>
 __global__ void k_band(const TileInfo* __restrict__ tiles, int64_t ngroups, const float* __restrict__ pt_tau,
                        const float* __restrict__ pt_tau_est, float* g_lt, unsigned long long* nband) {
   const int64_t grp = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
@@ -1307,7 +1316,8 @@ __global__ void k_seg_sums(int nseg, const int64_t* __restrict__ off, const doub
     for (int j = 0; j < 3; ++j) out[3 * seg + j] = s[j][0];
 }
 
-// log2 of the smallest per-point value of each 128-point tile (one warp per tile).
+// log2 of the smallest per-point value of each tile (one warp per tile).
+template <int kPPT>
 __global__ void k_tile_min_log2(const TileInfo* __restrict__ tiles, int64_t nwt, const float* __restrict__ pt,
                                 float* lt) {
   const int64_t wt = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + (threadIdx.x >> 5);
@@ -1479,11 +1489,12 @@ int sample_stride_for(int64_t ngrid) {
 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
 // permutation (sorted position -> grid index) and the tile / sub-tile boxes.
-int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, DevBuf<float4>& phi,
+int sort_points(inca_ctx* c, int64_t stride, int ppt, const double lo[3], double inv, DevBuf<float4>& phi,
                 DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, DevBuf<TileInfo>& tiles,
                 int64_t* n_out, int64_t* ntiles_out, std::vector<MolSpan>& spans) {
   const int64_t n = (c->ngrid + stride - 1) / stride;
-  // tiles of <= 128 consecutive sorted points; in a batch they never straddle two molecules
+  const int64_t tile = 32 * static_cast<int64_t>(ppt);
+  // tiles of <= 32 ppt consecutive sorted points; in a batch they never straddle two molecules
   std::vector<TileInfo> ht;
   const bool batch = c->batch_molecules > 0;
   const int nmol = batch ? c->batch_molecules : 1;
@@ -1496,13 +1507,13 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
       cnt = (b + stride - 1) / stride - (a + stride - 1) / stride;
     }
     spans[m] = MolSpan{static_cast<int64_t>(ht.size()), 0, o, cnt};
-    for (int64_t t = 0; t < cnt; t += kWarpTile)
-      ht.push_back(TileInfo{o + t, static_cast<int>(std::min<int64_t>(kWarpTile, cnt - t)), m});
+    for (int64_t t = 0; t < cnt; t += tile)
+      ht.push_back(TileInfo{o + t, static_cast<int>(std::min<int64_t>(tile, cnt - t)), m});
     spans[m].ntiles = static_cast<int64_t>(ht.size()) - spans[m].tile0;
     o += cnt;
   }
   const int64_t nwt = static_cast<int64_t>(ht.size());
-  if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * kPPT) ||
+  if (phi.reserve(n) || plo.reserve(n) || perm.reserve(n) || boxes.reserve(8 * nwt + 8 * nwt * ppt) ||
       tiles.reserve(std::max<int64_t>(nwt, 1)))
     return set_error(c, INCA_E_NOMEM, "sorted grid");
   if (nwt) INCA_CUDA(c, cudaMemcpyAsync(tiles.p, ht.data(), sizeof(TileInfo) * nwt, cudaMemcpyHostToDevice, c->stream));
@@ -1531,8 +1542,13 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
   e = cub::DeviceRadixSort::SortPairs(tmp, tb, k1, k2, i1, perm.p, n, 0, 63, c->stream);
   if (!e) {
     INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, phi.p, plo.p);
-    INCA_LAUNCH(c, k_boxes, static_cast<unsigned>((nwt + 7) / 8), 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p,
-                boxes.p + 8 * nwt);
+    const unsigned bb = static_cast<unsigned>((nwt + 7) / 8);
+    if (ppt == 3)
+      INCA_LAUNCH(c, k_boxes<3>, bb, 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p, boxes.p + 8 * nwt);
+    else if (ppt == 5)
+      INCA_LAUNCH(c, k_boxes<5>, bb, 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p, boxes.p + 8 * nwt);
+    else
+      INCA_LAUNCH(c, k_boxes<4>, bb, 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p, boxes.p + 8 * nwt);
     e = cudaStreamSynchronize(c->stream);  // the host tile table above is stack-owned
   }
   if (e) return cuda_error(c, e, "sorted grid");
@@ -1542,9 +1558,9 @@ int sort_points(inca_ctx* c, int64_t stride, const double lo[3], double inv, Dev
 }
 
 // The sorted grid (and, for the one-pass form, the sorted sample), rebuilt when the grid changes.
-int prepare_sorted_grid(inca_ctx* c, bool sample) {
+int prepare_sorted_grid(inca_ctx* c, bool sample, int ppt) {
   const int stride = c->tune_sample_stride > 0 ? c->tune_sample_stride : sample_stride_for(c->ngrid);
-  const bool main_ok = c->mix_version == c->grid_version;
+  const bool main_ok = c->mix_version == c->grid_version && c->mix_ppt == ppt;
   const bool sample_ok = !sample || (c->sample_version == c->grid_version && c->sample_stride_built == stride);
   if (main_ok && sample_ok) return INCA_OK;
   const int64_t n = c->ngrid;
@@ -1559,13 +1575,14 @@ int prepare_sorted_grid(inca_ctx* c, bool sample) {
   const double inv = 2097151.0 / ext;
   int64_t nn = 0;
   if (!main_ok) {
-    const int st = sort_points(c, 1, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
+    const int st = sort_points(c, 1, ppt, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
                                &c->ntiles, c->mol_span);
     if (st) return st;
     c->mix_version = c->grid_version;
+    c->mix_ppt = ppt;
   }
   if (!sample_ok) {
-    const int st = sort_points(c, stride, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
+    const int st = sort_points(c, stride, kSamplePPT, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
                                c->d_tiles_s, &c->nsample, &c->ntiles_s, c->mol_span_s);
     if (st) return st;
     c->sample_version = c->grid_version;
@@ -1632,11 +1649,17 @@ unsigned persistent_ctas(int64_t nitems, int num_sms, int ctas_per_sm = INCA_PAS
       std::max<int64_t>(1, std::min<int64_t>(nitems, static_cast<int64_t>(num_sms) * ctas_per_sm)));
 }
 
-// The register budgets the one-pass kernel is compiled for (resident one-warp CTAs per SM);
-// the schedule (inca_set_tuning, inca_autotune) picks one.
-bool valid_pass_ctas(int n) { return n == 12 || n == 16 || n == 20; }
-
 }  // namespace
+
+// The shapes the one-pass kernel is compiled for: points per lane (tile of 32 ppt points) and
+// register budget (resident one-warp CTAs per SM); the schedule (inca_set_tuning,
+// inca_autotune) picks one. Five points per lane need the larger budgets, three the smaller.
+bool valid_pass_shape(int ppt, int ctas) {
+  if (ppt == 4) return ctas == 12 || ctas == 16 || ctas == 20;
+  if (ppt == 3) return ctas == 16 || ctas == 20;
+  if (ppt == 5) return ctas == 12 || ctas == 16;
+  return false;
+}
 
 namespace {
 
@@ -1655,6 +1678,7 @@ struct MixedPlan {
   bool fused = false;
   int mode = 2, nseg = 1, emode = 0, nmol = 1, cheap = 1, wait_test = 0;
   int ctas = INCA_PASS_CTAS_PER_SM;  // resident CTAs per SM of the one-pass kernel (its register budget)
+  int ppt = kDefaultPPT;             // points per lane of the main grid's tiles
   bool f64 = false;  // the screened FP64 form (k_pass_f64 instead of the FP32 passes)
   const int* seg_of = nullptr;
   int64_t ngrid = 0, nwt = 0, ngroups = 0, nitems = 0, npart = 0, ndrop = 0;
@@ -1679,7 +1703,17 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   const double fuse_min = env_knob("INCA_FUSE_MIN_POINTS", static_cast<double>(kFuseMinPoints), 256.0, HUGE_VAL);
   P.fused = (c->grid_kind == GRID_RADIAL || c->grid_kind == GRID_SCAN || c->grid_kind == GRID_CUBE) &&
             static_cast<double>(ngrid) >= fuse_min;
-  int st = prepare_sorted_grid(c, P.fused);
+  // test of the bounded staging waits: the pass-1 kernels start no copy and give up waiting
+  // after this many tries (0: off)
+  P.wait_test = static_cast<int>(env_knob("INCA_TEST_STAGE_TIMEOUT", 0.0, 0.0, 1e6));
+  // the shape of the one-pass kernel (the two-pass form and the wait test use the default)
+  const int tppt = c->tune_ppt > 0 ? c->tune_ppt : kDefaultPPT;
+  const int tctas = c->tune_ctas > 0 ? c->tune_ctas : INCA_PASS_CTAS_PER_SM;
+  if (P.fused && P.wait_test == 0 && valid_pass_shape(tppt, tctas)) {
+    P.ppt = tppt;
+    P.ctas = tctas;
+  }
+  int st = prepare_sorted_grid(c, P.fused, P.ppt);
   if (st) return st;
   P.eps = eps;
   // knobs (environment, read per evaluation; tuning and test aids)
@@ -1695,13 +1729,9 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
                                                                                            : kCheapSlack,
                                               0.0, 31.0));
   P.cheap = env_knob("INCA_CHEAP_TIER", 1.0, 0.0, 2.0) >= 0.5 ? 1 + slack : 0;
-  // test of the bounded staging waits: the pass-1 kernels start no copy and give up waiting
-  // after this many tries (0: off)
-  P.wait_test = static_cast<int>(env_knob("INCA_TEST_STAGE_TIMEOUT", 0.0, 0.0, 1e6));
   P.nwt = c->ntiles;
-  P.ngroups = P.nwt * kPPT;
+  P.ngroups = P.nwt * P.ppt;
   const int ipc = c->tune_items_per_cta > 0 ? c->tune_items_per_cta : kItemsPerCta;
-  P.ctas = valid_pass_ctas(c->tune_ctas) && P.fused ? c->tune_ctas : INCA_PASS_CTAS_PER_SM;
   const std::vector<MolWork> hmw =
       work_table(c->mol_span, c->mol_chunks, c->num_sms, ipc, &P.nitems, &P.npart, &P.ndrop, P.ctas);
   P.nmol = static_cast<int>(hmw.size());
@@ -1809,8 +1839,10 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
 }
 
 // The device work of one evaluation (no host synchronisation: it can be captured in a graph).
-// ev (optional) gets events around the pass over all terms and the correction pass.
-int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
+// ev (optional) gets events around the pass over all terms and the correction pass. kPPT: points
+// per lane of the main grid's tiles (the sample's are always kSamplePPT).
+template <int kPPT>
+int mixed_launch_t(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   const int64_t ngrid = P.ngrid, nwt = P.nwt;
   const int nseg = P.nseg;
   const TileInfo* tiles = c->d_tiles.p;
@@ -1826,7 +1858,7 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   if (P.fused) {
     const int64_t ns = P.ns;
 #define INCA_PASS1_EST(T)                                                                                         \
-  INCA_LAUNCH(c, (k_pass1<false, true, INCA_PASS_CTAS_PER_SM, T>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws,     \
+  INCA_LAUNCH(c, (k_pass1<false, true, INCA_PASS_CTAS_PER_SM, T, kSamplePPT>), P.nctas_s, 32, P.dsmem, c->d_chunks.p, P.mws,     \
               P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi_s.p, c->d_plo_s.p, c->d_tiles_s.p, c->d_wtbox_s.p,     \
               P.nitems_s, P.stage_floats, nullptr, nullptr, nullptr, 0, P.q1, P.qabs, nullptr, P.work + 3,          \
               P.stats + 8, P.errw, P.wait_test)
@@ -1853,40 +1885,50 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
       INCA_LAUNCH(c, k_thr_est_max, 1, 32, 0, P.dmax, P.eps, P.tau_scale, P.safety, kCubeMargin, 0.5 * P.drop_frac,
                   P.nq, P.dTest, P.dTheta);
     }
-    INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTest, c->d_w.p,
+    INCA_LAUNCH(c, k_thresholds<kPPT>, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTest, c->d_w.p,
                 nullptr, nullptr, P.eps, P.tau_scale, nullptr, P.ptau_est);
     if (use_drop) {
-      INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTheta,
+      INCA_LAUNCH(c, k_thresholds<kPPT>, P.gblk, 256, 0, tiles, P.ngroups, P.emode, c->d_perm.p, P.seg_of, P.dTheta,
                   c->d_w.p, nullptr, nullptr, P.eps, P.tau_scale, nullptr, P.ptheta);
-      INCA_LAUNCH(c, k_tile_min_log2, P.tblk, 256, 0, tiles, nwt, P.ptheta, P.ltdrop);
+      INCA_LAUNCH(c, k_tile_min_log2<kPPT>, P.tblk, 256, 0, tiles, nwt, P.ptheta, P.ltdrop);
     }
   }
   // ---- the pass over all terms (one-pass form: corrections above the estimated thresholds,
   // terms below the drop thresholds left out)
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[1], c->stream));
   if (P.f64)
-    INCA_LAUNCH(c, k_pass_f64, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+    INCA_LAUNCH(c, k_pass_f64<kPPT>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, use_drop ? P.ltdrop : nullptr, P.p1,
                 P.pabs, use_drop ? P.dmass : nullptr, P.work, P.stats, P.errw);
   else if (P.fused) {
-#define INCA_PASS1_FUSED(N)                                                                                       \
-  INCA_LAUNCH(c, (k_pass1<true, false, N>), P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,    \
-              c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, P.ptau_est, P.tab,      \
-              use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats, P.errw, P.wait_test)
-    if (P.wait_test > 0)
-      INCA_LAUNCH(c, (k_pass1<true, false, INCA_PASS_CTAS_PER_SM, true>), P.nctas, 32, P.dsmem, c->d_chunks.p,
-                  P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems,
-                  P.stage_floats, P.ptau_est, P.tab, use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass,
-                  P.work, P.stats, P.errw, P.wait_test);
-    else if (P.ctas == 12)
-      INCA_PASS1_FUSED(12);
-    else if (P.ctas == 20)
-      INCA_PASS1_FUSED(20);
-    else
-      INCA_PASS1_FUSED(16);
+#define INCA_PASS1_FUSED(N, T)                                                                                    \
+  INCA_LAUNCH(c, (k_pass1<true, false, N, T, kPPT>), P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol,          \
+              c->d_classes.p, c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats,         \
+              P.ptau_est, P.tab, use_drop ? P.ltdrop : nullptr, P.cheap, P.p1, P.pabs, P.dmass, P.work, P.stats,    \
+              P.errw, P.wait_test)
+    // the shapes valid_pass_shape admits (the wait test runs at the default shape only)
+    if constexpr (kPPT == kDefaultPPT) {
+      if (P.wait_test > 0)
+        INCA_PASS1_FUSED(INCA_PASS_CTAS_PER_SM, true);
+      else if (P.ctas == 12)
+        INCA_PASS1_FUSED(12, false);
+      else if (P.ctas == 20)
+        INCA_PASS1_FUSED(20, false);
+      else
+        INCA_PASS1_FUSED(16, false);
+    } else if constexpr (kPPT == 3) {
+      if (P.ctas == 20)
+        INCA_PASS1_FUSED(20, false);
+      else
+        INCA_PASS1_FUSED(16, false);
+    } else {
+      if (P.ctas == 12)
+        INCA_PASS1_FUSED(12, false);
+      else
+        INCA_PASS1_FUSED(16, false);
+    }
 #undef INCA_PASS1_FUSED
-  }
-  else
+  } else if constexpr (kPPT == kDefaultPPT) {  // the two-pass form: default shape only
     if (P.wait_test > 0)
       INCA_LAUNCH(c, (k_pass1<false, false, INCA_PASS_CTAS_PER_SM, true>), P.nctas, 32, P.dsmem, c->d_chunks.p,
                   P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems,
@@ -1896,6 +1938,9 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
       INCA_LAUNCH(c, k_pass1<false>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p,
                   c->d_rec32.p, c->d_phi.p, c->d_plo.p, tiles, wbox, P.nitems, P.stage_floats, nullptr, nullptr,
                   nullptr, 0, P.p1, P.pabs, nullptr, P.work, P.stats, P.errw, 0);
+  } else {
+    return set_error(c, INCA_E_STATE, "inca_eval: the two-pass form runs at the default tile shape");
+  }
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[2], c->stream));
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.p1, nullptr, P.Is);
   INCA_LAUNCH(c, k_sum_mol, nblk32(ngrid), kSumBlock, 0, ngrid, P.mwdev, P.nmol, P.pabs, nullptr, P.Ms);
@@ -1924,14 +1969,14 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   } else {
     INCA_CUDA(c, cudaMemsetAsync(P.dT, 0, sizeof(double), c->stream));
   }
-  INCA_LAUNCH(c, k_thresholds, P.gblk, 256, 0, tiles, P.ngroups, P.mode, c->d_perm.p, P.seg_of, P.dT, c->d_w.p, P.Is,
+  INCA_LAUNCH(c, k_thresholds<kPPT>, P.gblk, 256, 0, tiles, P.ngroups, P.mode, c->d_perm.p, P.seg_of, P.dT, c->d_w.p, P.Is,
               P.Ms, P.eps, P.tau_scale, P.fused ? nullptr : P.glt, P.ptau);
   // sub-tiles where an exact threshold fell below its estimate (the correction pass skips
   // every item whose tile has none)
-  if (P.fused) INCA_LAUNCH(c, k_band, P.gblk, 256, 0, tiles, P.ngroups, P.ptau, P.ptau_est, P.glt, P.stats + 12);
+  if (P.fused) INCA_LAUNCH(c, k_band<kPPT>, P.gblk, 256, 0, tiles, P.ngroups, P.ptau, P.ptau_est, P.glt, P.stats + 12);
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[3], c->stream));
   if (!P.f64) {  // the screened FP64 form has nothing to correct
-    INCA_LAUNCH(c, k_pass2, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
+    INCA_LAUNCH(c, k_pass2<kPPT>, P.nctas, 32, P.dsmem, c->d_chunks.p, P.mwdev, P.nmol, c->d_classes.p, c->d_rec32.p,
                 c->d_phi.p, c->d_plo.p, tiles, wbox, gbox, P.glt, P.ptau, P.fused ? P.ptau_est : nullptr,
                 use_drop ? P.ltdrop : nullptr, P.cheap, P.tab, P.nitems, P.stage_floats, P.p2, P.work + 1,
                 P.stats + 4, P.errw);
@@ -1943,6 +1988,14 @@ int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
   if (ev) INCA_CUDA(c, cudaEventRecord(ev->e[5], c->stream));
   INCA_CUDA(c, cudaGetLastError());
   return INCA_OK;
+}
+
+int mixed_launch(inca_ctx* c, const MixedPlan& P, bool use_drop, Events* ev) {
+  switch (P.ppt) {
+    case 3: return mixed_launch_t<3>(c, P, use_drop, ev);
+    case 5: return mixed_launch_t<5>(c, P, use_drop, ev);
+    default: return mixed_launch_t<kDefaultPPT>(c, P, use_drop, ev);
+  }
 }
 
 // After the device work: errors, the retry flag, statistics and (with events) timings.
@@ -2066,14 +2119,15 @@ int eval_fp64_screened(inca_ctx* c, double eps, bool* plain) {
 // fastest stays in the context. All candidates meet the tolerance, so the choice changes only
 // the time. On an error the context's previous schedule is restored.
 int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_out, double* safety_out,
-                   double* drop_out, int* ctas_out, int* slack_out, double* best_ms, double* default_ms) {
+                   double* drop_out, int* ctas_out, int* slack_out, int* ppt_out, double* best_ms,
+                   double* default_ms) {
   struct Sched {
     int ipc, stride;
     double safety, drop;
-    int ctas, slack;
+    int ctas, slack, ppt;
   };
   const Sched saved{c->tune_items_per_cta, c->tune_sample_stride, c->tune_safety, c->tune_drop, c->tune_ctas,
-                    c->tune_cheap_slack};
+                    c->tune_cheap_slack, c->tune_ppt};
   auto apply = [&](const Sched& s) {
     c->tune_items_per_cta = s.ipc;
     c->tune_sample_stride = s.stride;
@@ -2081,6 +2135,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     c->tune_drop = s.drop;
     c->tune_ctas = s.ctas;
     c->tune_cheap_slack = s.slack;
+    c->tune_ppt = s.ppt;
   };
   auto timed = [&](const Sched& s, double* ms) -> int {
     apply(s);
@@ -2097,7 +2152,8 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     *ms = t[t.size() / 2];
     return INCA_OK;
   };
-  Sched cur{kItemsPerCta, sample_stride_for(c->ngrid), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, kCheapSlack};
+  Sched cur{kItemsPerCta, sample_stride_for(c->ngrid), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, kCheapSlack,
+            kDefaultPPT};
   double best = 0.0;
   int st = timed(cur, &best);
   if (st) return st;
@@ -2106,7 +2162,8 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   const int strides[] = {8, 16, 32, 64};
   const double safeties[] = {0.3, 0.5, 0.7, 1.0, 1.25};
   const double drops[] = {0.02, 0.05, 0.1, 0.2, 0.3};
-  const int ctass[] = {12, 16, 20};
+  // the kernel's shape: (points per lane, resident CTAs per SM), the pairs valid_pass_shape admits
+  const int shapes[][2] = {{4, 16}, {4, 12}, {4, 20}, {3, 16}, {3, 20}, {5, 12}, {5, 16}};
   const int slacks[] = {0, 2, 4, 6, 8};
   auto consider = [&](Sched s) -> int {
     double ms;
@@ -2119,18 +2176,25 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     return INCA_OK;
   };
   for (int pass = 0; pass < 2; ++pass) {
-    for (int v : ctass)
-      if (v != cur.ctas && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, v, cur.slack}))) return st;
+    for (const auto& v : shapes)
+      if ((v[0] != cur.ppt || v[1] != cur.ctas) &&
+          (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, v[1], cur.slack, v[0]})))
+        return st;
     for (int v : ipcs)
-      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop, cur.ctas, cur.slack}))) return st;
+      if (v != cur.ipc && (st = consider({v, cur.stride, cur.safety, cur.drop, cur.ctas, cur.slack, cur.ppt})))
+        return st;
     for (int v : strides)
-      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop, cur.ctas, cur.slack}))) return st;
+      if (v != cur.stride && (st = consider({cur.ipc, v, cur.safety, cur.drop, cur.ctas, cur.slack, cur.ppt})))
+        return st;
     for (double v : safeties)
-      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop, cur.ctas, cur.slack}))) return st;
+      if (v != cur.safety && (st = consider({cur.ipc, cur.stride, v, cur.drop, cur.ctas, cur.slack, cur.ppt})))
+        return st;
     for (double v : drops)
-      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v, cur.ctas, cur.slack}))) return st;
+      if (v != cur.drop && (st = consider({cur.ipc, cur.stride, cur.safety, v, cur.ctas, cur.slack, cur.ppt})))
+        return st;
     for (int v : slacks)
-      if (v != cur.slack && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, cur.ctas, v}))) return st;
+      if (v != cur.slack && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, cur.ctas, v, cur.ppt})))
+        return st;
   }
   apply(cur);
   *ipc_out = cur.ipc;
@@ -2139,6 +2203,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
   *drop_out = cur.drop;
   *ctas_out = cur.ctas;
   *slack_out = cur.slack;
+  *ppt_out = cur.ppt;
   *best_ms = best;
   return INCA_OK;
 }
@@ -2151,7 +2216,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
 static std::vector<double> plan_signature(const inca_ctx* c, const MixedPlan& P) {
   auto a = [](const void* p) { return static_cast<double>(reinterpret_cast<uintptr_t>(p)); };
   std::vector<double> s = {double(P.fused), double(P.mode), double(P.nseg), double(P.emode), double(P.nmol),
-                           double(P.cheap), double(P.wait_test), double(P.ctas),
+                           double(P.cheap), double(P.wait_test), double(P.ctas), double(P.ppt),
                            a(P.seg_of), double(P.ngrid), double(P.nwt), double(P.ngroups), double(P.nitems),
                            double(P.npart), double(P.ndrop), double(P.ns), double(P.nitems_s), double(P.npart_s),
                            double(P.nctas), double(P.nctas_s), double(P.gblk), double(P.tblk),

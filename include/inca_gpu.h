@@ -155,8 +155,10 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
  * the stride of the grid sample that estimates the thresholds, the factor applied to the
  * estimates, the share of the tolerance given to left-out (quartet, tile) pairs
  * (drop_fraction, below 0.5; < 0: the default 0.1), and the register budget of the one-pass
- * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20, one compiled
- * instantiation each; 0: the default 16), and the slack of the cheap tier (cheap_slack, 0..30:
+ * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20; 0: the default 16) with
+ * the points each lane of its warp tiles holds (points_per_lane: 3, 4 or 5; 0: the default 4;
+ * the pairs compiled are (4, 12|16|20), (3, 16|20) and (5, 12|16), any other pair is
+ * INCA_E_ARG), and the slack of the cheap tier (cheap_slack, 0..30:
  * a (quartet, tile) pair is evaluated in plain FP32 when its rigorous error bound is at most
  * 2^cheap_slack times the tile's drop threshold; that bound joins the left-out mass, which is
  * checked after the pass as before, so a large slack can cost a repeat, never accuracy). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
@@ -173,6 +175,7 @@ typedef struct inca_tuning {
   double drop_fraction;
   int32_t ctas_per_sm;
   int32_t cheap_slack;
+  int32_t points_per_lane;
 } inca_tuning;
 int inca_autotune(inca_ctx* ctx, double tol, int32_t reps, inca_tuning* chosen);
 int inca_set_tuning(inca_ctx* ctx, const inca_tuning* tuning);

@@ -172,7 +172,8 @@ def test_autotune_keeps_tolerance(ctx, scan_fp64):
     assert t["sample_stride"] in (8, 16, 32, 64)
     assert t["estimate_safety"] in (0.3, 0.5, 0.7, 1.0, 1.25)
     assert t["drop_fraction"] in (0.02, 0.05, 0.1, 0.2, 0.3)
-    assert t["ctas_per_sm"] in (12, 16, 20)
+    assert (t["points_per_lane"], t["ctas_per_sm"]) in ((4, 12), (4, 16), (4, 20), (3, 16), (3, 20), (5, 12),
+                                                        (5, 16))
     assert t["cheap_slack"] in (0, 2, 4, 6, 8)
     assert 0 < t["best_ms"] <= t["default_ms"]
     try:
@@ -180,12 +181,18 @@ def test_autotune_keeps_tolerance(ctx, scan_fp64):
         I = _scan_mixed(ctx)
         rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
         assert rel.max() <= 1e-8, rel.max()
-        for ipc, stride, safety, drop, ctas, slack in ((4, 32, 0.3, 0.2, 12, 8), (48, 8, 0.7, 0.02, 20, 0),
-                                                      (12, 16, 0.5, 0.05, 16, 30)):
-            ctx.set_tuning(ipc, stride, safety, drop, ctas, slack)
+        for ipc, stride, safety, drop, ctas, slack, ppt in ((4, 32, 0.3, 0.2, 12, 8, 4), (48, 8, 0.7, 0.02, 20, 0, 3),
+                                                           (12, 16, 0.5, 0.05, 16, 30, 5), (24, 16, 0.7, 0.1, 16, 4, 3),
+                                                           (24, 32, 0.7, 0.1, 12, 4, 5)):
+            ctx.set_tuning(ipc, stride, safety, drop, ctas, slack, ppt)
             I = _scan_mixed(ctx)
             rel = np.abs(I - scan_fp64) / np.abs(scan_fp64)
             assert rel.max() <= 1e-8, (ipc, stride, safety, rel.max())
+        # a tile shape that is not compiled (five points per lane need the larger register budgets)
+        from inca_parallel_gb300 import IncaError
+        for ctas, ppt in ((20, 5), (12, 3), (16, 6)):
+            with pytest.raises(IncaError, match="INCA_E_ARG"):
+                ctx.set_tuning(24, 16, 0.7, 0.1, ctas, 4, ppt)
     finally:
         ctx.set_tuning()
 
@@ -199,10 +206,12 @@ def test_graph_follows_schedule_knobs_and_reprepare(ctx, monkeypatch):
     ctx.eval_graph(mode=1, tol=1e-8)
     np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), ref)
     try:
-        ctx.set_tuning(4, 32, 0.7, 0.1)
-        eager = ctx.eval(mode=1, tol=1e-8)
-        for _ in range(2):
-            np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
+        # a new schedule, then a new tile shape (the sorted grid is rebuilt with 160-point tiles)
+        for tune in ((4, 32, 0.7, 0.1), (24, 16, 0.7, 0.1, 16, 4, 5)):
+            ctx.set_tuning(*tune)
+            eager = ctx.eval(mode=1, tol=1e-8)
+            for _ in range(2):
+                np.testing.assert_array_equal(ctx.eval_graph(mode=1, tol=1e-8), eager)
     finally:
         ctx.set_tuning()
     monkeypatch.setenv("INCA_DROP_FRACTION", "0")
