@@ -55,6 +55,8 @@ namespace {
 // picks 3, 4 or 5; the grid sample behind the threshold estimates always uses 4.
 constexpr int kDefaultPPT = 4;
 constexpr int kSamplePPT = 4;
+// the default is 3 up to kFewRecords surviving records per molecule and 5 from kManyRecords
+constexpr double kFewRecords = 1e6, kManyRecords = 1e7;
 constexpr int kMaxStride32 = (12 + 2 * 3 * kMaxCoef + 3) & ~3;
 // tau = kTauScale (eps |O|)^2 / E_O: the error of an uncorrected term is a sum of independent
 // round-to-nearest errors bounded in total by e_t, so its variance is <= e_t^2 / 3, and
@@ -1649,6 +1651,16 @@ unsigned persistent_ctas(int64_t nitems, int num_sms, int ctas_per_sm = INCA_PAS
       std::max<int64_t>(1, std::min<int64_t>(nitems, static_cast<int64_t>(num_sms) * ctas_per_sm)));
 }
 
+// Points per lane of the one-pass kernel when the schedule sets none, from the mean surviving
+// records per molecule. Measured at the default schedule otherwise (16 CTAs per SM): CH4
+// (1.1e5 records; radial integrals at 3 050 and 30 200 points, I(s) at 31 490 and 118 000)
+// and ten small batch molecules ran 1-10% faster at 3 than at 4 and slower at 5; the 12-atom
+// ring (5.1e7 records; 89 614 and 345 876 points) ran 5-7% faster at 5 and slower at 3.
+int default_ppt(const inca_ctx* c) {
+  const double per_mol = static_cast<double>(c->nsurv) / std::max<size_t>(1, c->mol_chunks.size());
+  return per_mol <= kFewRecords ? 3 : per_mol >= kManyRecords ? 5 : kDefaultPPT;
+}
+
 }  // namespace
 
 // The shapes the one-pass kernel is compiled for: points per lane (tile of 32 ppt points) and
@@ -1707,8 +1719,9 @@ int mixed_plan(inca_ctx* c, double eps, MixedPlan& P) {
   // after this many tries (0: off)
   P.wait_test = static_cast<int>(env_knob("INCA_TEST_STAGE_TIMEOUT", 0.0, 0.0, 1e6));
   // the shape of the one-pass kernel (the two-pass form and the wait test use the default)
-  const int tppt = c->tune_ppt > 0 ? c->tune_ppt : kDefaultPPT;
+  int tppt = c->tune_ppt > 0 ? c->tune_ppt : default_ppt(c);
   const int tctas = c->tune_ctas > 0 ? c->tune_ctas : INCA_PASS_CTAS_PER_SM;
+  if (c->tune_ppt <= 0 && !valid_pass_shape(tppt, tctas)) tppt = kDefaultPPT;  // the budget asked for
   if (P.fused && P.wait_test == 0 && valid_pass_shape(tppt, tctas)) {
     P.ppt = tppt;
     P.ctas = tctas;
@@ -2153,7 +2166,7 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
     return INCA_OK;
   };
   Sched cur{kItemsPerCta, sample_stride_for(c->ngrid), kEstSafety, kDropFrac, INCA_PASS_CTAS_PER_SM, kCheapSlack,
-            kDefaultPPT};
+            default_ppt(c)};
   double best = 0.0;
   int st = timed(cur, &best);
   if (st) return st;

@@ -156,13 +156,15 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
  * estimates, the share of the tolerance given to left-out (quartet, tile) pairs
  * (drop_fraction, below 0.5; < 0: the default 0.1), and the register budget of the one-pass
  * kernel as resident one-warp CTAs per SM (ctas_per_sm: 12, 16 or 20; 0: the default 16) with
- * the points each lane of its warp tiles holds (points_per_lane: 3, 4 or 5; 0: the default 4;
- * the pairs compiled are (4, 12|16|20), (3, 16|20) and (5, 12|16), any other pair is
- * INCA_E_ARG), and the slack of the cheap tier (cheap_slack, 0..30:
+ * the points each lane of its warp tiles holds (points_per_lane: 3, 4 or 5; the pairs compiled
+ * are (4, 12|16|20), (3, 16|20) and (5, 12|16), any other pair is INCA_E_ARG; 0: from the mean
+ * surviving records per molecule, 3 up to 1e6, 5 from 1e7, else 4, and 4 where that value does
+ * not pair with ctas_per_sm), and the slack of the cheap tier (cheap_slack, 0..30:
  * a (quartet, tile) pair is evaluated in plain FP32 when its rigorous error bound is at most
  * 2^cheap_slack times the tile's drop threshold; that bound joins the left-out mass, which is
- * checked after the pass as before, so a large slack can cost a repeat, never accuracy). inca_autotune times complete INCA_MIXED evaluations of the current grid and records
- * (median of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
+ * checked after the pass as before, so a large slack can cost a repeat, never accuracy).
+ * inca_autotune times complete INCA_MIXED evaluations of the current grid and records (median
+ * of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
  * context and reports it with the time of the default schedule; the last evaluation's results
  * stay on the device. inca_set_tuning sets a schedule (NULL: the defaults). Every schedule meets
  * the tolerance. No counterpart in the reference. */
