@@ -1653,7 +1653,7 @@ unsigned persistent_ctas(int64_t nitems, int num_sms, int ctas_per_sm = INCA_PAS
 
 // Points per lane of the one-pass kernel when the schedule sets none, from the mean surviving
 // records per molecule. Measured at the default schedule otherwise (16 CTAs per SM): CH4
-// (1.1e5 records; radial integrals at 3 050 and 30 200 points, I(s) at 31 490 and 118 000)
+// (1.1e5 records; radial integrals at 3 050 and 30 200 points, I(s) at 31 490 and 62 390)
 // and ten small batch molecules ran 1-10% faster at 3 than at 4 and slower at 5; the 12-atom
 // ring (5.1e7 records; 89 614 and 345 876 points) ran 5-7% faster at 5 and slower at 3.
 int default_ppt(const inca_ctx* c) {
