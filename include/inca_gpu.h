@@ -312,9 +312,8 @@ int inca_mlp_train(inca_mlp* mlp, int64_t n, const float* X, const float* T, int
  *  - npts <= INCA_NOALLOC_MAX_POINTS; a larger npts returns INCA_E_LIMIT and queues nothing.
  *    The intermediate sums live in a fixed 16 MiB device array inside the library.
  *  - The first call on a device sets that device up (it looks up the address of the fixed
- *    array in the current CUDA context); make that first call before any stream capture
- *    begins. A call made under a different context than the last one on that device (for
- *    instance after cudaDeviceReset) sets the device up again, and the same rule applies.
+ *    array in the current CUDA context). A call made under a different context than the last
+ *    one on that device (for instance after cudaDeviceReset) sets the device up again.
  *  - Calls that overlap in time on one device (different streams or host threads) share the
  *    fixed array and race: order them, e.g. on one stream.
  *  - nrec == 0 writes zeros to ivec with one cudaMemsetAsync on `stream`.
