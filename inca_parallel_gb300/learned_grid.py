@@ -15,7 +15,7 @@ centre solves: for the centre's Gaussian components, the scale that minimises th
 Gauss-Legendre error of their radial integrals (int r^2 exp(-e r^2) dr over the mapped rule) at a
 given nrad, and the smallest nrad whose best error is below the target. Autogrid's centres and
 Ps stay; its scale and the caller's nrad stay the fallback where the features leave the training
-range or a prediction leaves its bounds. The judge of a grid is the radial integral against a
+range or a prediction leaves its bounds. A grid is measured by its radial integral against a
 dense reference grid (nrad 150, nang 974) computed by the engine itself.
 """
 import math
@@ -213,7 +213,7 @@ def mlp_reference(params, nin, nh, nout, X, T=None):
     return y, loss, g
 
 
-def judge(lg, cases, nrad=50, nang=302, dense=(150, 974), nohydro=True, ctx=None):
+def compare_with_dense(lg, cases, nrad=50, nang=302, dense=(150, 974), nohydro=True, ctx=None):
     """Radial integrals of each case (basis, ijkl, v) on autogrid's grid and on the learned grid
     (learned scales and node counts), both against a dense autogrid grid; returns one dict per
     case with the relative errors and the point counts."""
@@ -272,7 +272,7 @@ def targets_3d(ctx, cent, Ps, alf, nrad, nang=302, dense=(150, 974), mults=MULTS
     return np.log(np.asarray(mults)[np.argmin(errs, axis=0)]), errs
 
 
-def _judge_molecule(rng, natoms_range=(2, 7), nprim_range=(10, 36)):
+def _dense_case_molecule(rng, natoms_range=(2, 7), nprim_range=(10, 36)):
     """A seeded molecule with s and p primitives of exponents up to 50 (where the reference's
     polynomial fit is exact) and its closed-shell 1-RDM."""
     from . import workloads as W
@@ -292,7 +292,7 @@ def training_set_3d(ctx, nmol=60, seed=20261208, nrad_set=(30, 50), nang=302):
     rng = np.random.default_rng(seed)
     X, Y = [], []
     for _ in range(nmol):
-        b, D = _judge_molecule(rng)
+        b, D = _dense_case_molecule(rng)
         ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
         ctx.gen_closed_shell_dm2(D, unique=True)
         ctx.prepare(1e-12)
@@ -306,7 +306,7 @@ def training_set_3d(ctx, nmol=60, seed=20261208, nrad_set=(30, 50), nang=302):
     return np.vstack(X), np.vstack(Y)
 
 
-def judge_equal_points(lg, cases, nrads=(30, 50), nang=302, dense=(150, 974), ctx=None):
+def compare_at_equal_points(lg, cases, nrads=(30, 50), nang=302, dense=(150, 974), ctx=None):
     """Per case and nrad: the radial-integral error against the dense grid with autogrid's scales
     and with the learned scales, both with nrad nodes on every centre (equal points)."""
     from . import Context, centercalc
@@ -351,7 +351,7 @@ def level_study(ctx, nmol=20, seed=4242, levels=LEVELS, auto=(50, 302), dense=(1
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(nmol):
-        b, D = _judge_molecule(rng, natoms_range=(2, 9), nprim_range=(10, 60))
+        b, D = _dense_case_molecule(rng, natoms_range=(2, 9), nprim_range=(10, 60))
         ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
         ctx.gen_closed_shell_dm2(D, unique=True)
         ctx.prepare(1e-12)
@@ -377,7 +377,7 @@ def level_study(ctx, nmol=20, seed=4242, levels=LEVELS, auto=(50, 302), dense=(1
 
 
 def main(argv=None):
-    """Train on autogrid's centres for 500 seeded geometries of 2-20 atoms and judge the learned
+    """Train on autogrid's centres for 500 seeded geometries of 2-20 atoms and compare the learned
     grids against dense grids (nrad 150, nang 974) on held-out molecules with real DM2s:
         python -m inca_parallel_gb300.learned_grid [nmol] [out.npz]"""
     import json
@@ -404,7 +404,7 @@ def main(argv=None):
         D, _ = W.closed_shell_density(b, nocc, int(rng.integers(1 << 30)))
         ijkl, v = W.folded_records(D)
         cases.append((b, ijkl, v))
-    res = judge(lg, cases)
+    res = compare_with_dense(lg, cases)
     print(json.dumps({"molecules": nmol, "samples": len(X), "targets_s": t1 - t0, "train_s": t2 - t1,
                       "train_loss": loss, "held_out": res}, indent=1))
 

@@ -87,7 +87,7 @@ def test_per_centre_dense_grid_targets():
     # multiplier serves every centre, and each centre's target is its own best multiplier
     from inca_parallel_gb300 import Context, centercalc
     rng = np.random.default_rng(12)
-    b, D = LG._judge_molecule(rng, natoms_range=(3, 4), nprim_range=(12, 16))
+    b, D = LG._dense_case_molecule(rng, natoms_range=(3, 4), nprim_range=(12, 16))
     with Context(0) as ctx:
         ctx.set_primitives(b["alpha"], b["tmn"], b["xyz"])
         ctx.gen_closed_shell_dm2(D, unique=True)
