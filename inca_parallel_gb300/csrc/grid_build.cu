@@ -142,6 +142,19 @@ __global__ void k_scan_candidates(int64_t ncand, const ScanShell* __restrict__ s
   keep[g] = k ? 1 : 0;
 }
 
+// Points kept on each shell of a scan grid (its candidates' keep flags summed): one warp per shell.
+__global__ void k_shell_counts(int nsh, const ScanShell* __restrict__ sh, const uint8_t* __restrict__ keep,
+                               int* counts) {
+  const int s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (s >= nsh) return;
+  const int lane = threadIdx.x & 31;
+  const ScanShell S = sh[s];
+  int k = 0;
+  for (int i = lane; i < S.nang; i += 32) k += keep[S.first + i];
+  for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+  if (lane == 0) counts[s] = k;
+}
+
 // Cube lattice (gridpoints3): x outer, y middle, z inner.
 __global__ void k_cube(int64_t n, double x0, double y0, double z0, double sx, double sy, double sz,
                        int ny, int nz, double* ox, double* oy, double* oz) {
@@ -450,10 +463,12 @@ int grid_scan_device(inca_ctx* c, int nblock, const double* start, const double*
   if (nsh == 0) return set_error(c, INCA_E_ARG, "inca_grid_scan: no shells");
   const size_t nlx = lx.size();
   ScanShell* dsh = nullptr;
+  int* dcnt = nullptr;
   double *dlx = nullptr, *dly = nullptr, *dlz = nullptr, *dlw = nullptr;
   Candidates cd;
   int st = carve_candidates(c, ncand, cd, [&](Slab& sl) {
     dsh = sl.take<ScanShell>(nsh);
+    dcnt = sl.take<int>(nsh);
     dlx = sl.take<double>(nlx);
     dly = sl.take<double>(nlx);
     dlz = sl.take<double>(nlx);
@@ -468,19 +483,16 @@ int grid_scan_device(inca_ctx* c, int nblock, const double* start, const double*
   if (!e) {
     INCA_LAUNCH(c, k_scan_candidates, nblk(ncand), 256, 0, ncand, dsh, nsh, dlx, dly, dlz, dlw, nosym, cd.x, cd.y,
                 cd.z, cd.w, cd.tag, cd.keep);
+    INCA_LAUNCH(c, k_shell_counts, static_cast<unsigned>((nsh + 7) / 8), 256, 0, nsh, dsh, cd.keep, dcnt);
     e = cudaGetLastError();
   }
   if (e) return cuda_error(c, e, "inca_grid_scan");
   int64_t n = 0;
   st = compact_into(c, ncand, cd, &n);
   if (st) return st;
-  // points per shell: the shell tags are sorted, count on the host from the Lebedev z's
+  // points per shell (counted on the device; the compaction above has synchronised the stream)
   c->h_smn.assign(nsh, 0);
-  {
-    std::vector<int> tags(n);
-    INCA_CUDA(c, cudaMemcpy(tags.data(), c->d_cmap.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < n; ++i) c->h_smn[tags[i]]++;
-  }
+  INCA_CUDA(c, cudaMemcpy(c->h_smn.data(), dcnt, sizeof(int) * nsh, cudaMemcpyDeviceToHost));
   c->h_radi = radi;
   c->nradi = nsh;
   c->grid_kind = GRID_SCAN;

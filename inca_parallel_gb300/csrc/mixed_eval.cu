@@ -34,6 +34,7 @@
 //   e_t > tau_g gets t_df - t_32 (t_32 recomputed by the same instruction sequence as in
 //   pass 1).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -1079,13 +1080,16 @@ k_pass2(const WorkChunk* __restrict__ chunks, const MolWork* __restrict__ mw, in
 // Morton keys of the points g = j * stride, j < n (stride 1: the whole grid). With pmol (a
 // batch) the molecule occupies the top 7 bits and each coordinate 19 bits, so the sort keeps
 // every molecule's points together.
+// bb: the grid's bounding box lo[3], hi[3] and the key scale 2^21 - 1 over its largest extent
+// (k_bbox), read on the device so that no host round trip separates the two kernels.
 __global__ void k_morton(int64_t n, int64_t stride, const double* __restrict__ px, const double* __restrict__ py,
-                         const double* __restrict__ pz, const int* __restrict__ pmol, double lo0, double lo1,
-                         double lo2, double inv, uint64_t* key, int64_t* idx) {
+                         const double* __restrict__ pz, const int* __restrict__ pmol,
+                         const double* __restrict__ bb, uint64_t* key, int64_t* idx) {
   const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (j >= n) return;
   const int64_t g = j * stride;
-  const double c[3] = {(px[g] - lo0) * inv, (py[g] - lo1) * inv, (pz[g] - lo2) * inv};
+  const double inv = bb[6];
+  const double c[3] = {(px[g] - bb[0]) * inv, (py[g] - bb[1]) * inv, (pz[g] - bb[2]) * inv};
   uint64_t k = 0;
   uint32_t q[3];
   for (int d = 0; d < 3; ++d) q[d] = static_cast<uint32_t>(fmin(fmax(c[d], 0.0), 2097151.0));
@@ -1152,6 +1156,10 @@ __global__ void __launch_bounds__(1024) k_bbox(int64_t n, const double* __restri
     __syncthreads();
   }
   if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x == 0) {
+    const double ext = fmax(fmax(sh[3][0] - sh[0][0], sh[4][0] - sh[1][0]), fmax(sh[5][0] - sh[2][0], 1e-12));
+    out[6] = 2097151.0 / ext;
+  }
 }
 
 // Bounding boxes (FP32, rounded outwards) of each tile of 32 kPPT points and its kPPT 32-point
@@ -1491,7 +1499,7 @@ int sample_stride_for(int64_t ngrid) {
 
 // Morton-sorted FP32 copy of the points g = j * stride of the grid (stride 1: all of it), the
 // permutation (sorted position -> grid index) and the tile / sub-tile boxes.
-int sort_points(inca_ctx* c, int64_t stride, int ppt, const double lo[3], double inv, DevBuf<float4>& phi,
+int sort_points(inca_ctx* c, int64_t stride, int ppt, DevBuf<float4>& phi,
                 DevBuf<float4>& plo, DevBuf<int64_t>& perm, DevBuf<float>& boxes, DevBuf<TileInfo>& tiles,
                 int64_t* n_out, int64_t* ntiles_out, std::vector<MolSpan>& spans) {
   const int64_t n = (c->ngrid + stride - 1) / stride;
@@ -1540,7 +1548,7 @@ int sort_points(inca_ctx* c, int64_t stride, int ppt, const double lo[3], double
   Carve cv{c->d_sscratch.p};
   layout(cv);
   INCA_LAUNCH(c, k_morton, nblk(n), 256, 0, n, stride, c->d_px.p, c->d_py.p, c->d_pz.p,
-              batch ? c->d_pmol.p : nullptr, lo[0], lo[1], lo[2], inv, k1, i1);
+              batch ? c->d_pmol.p : nullptr, c->d_bbox.p, k1, i1);
   e = cub::DeviceRadixSort::SortPairs(tmp, tb, k1, k2, i1, perm.p, n, 0, 63, c->stream);
   if (!e) {
     INCA_LAUNCH(c, k_gather_points, nblk(n), 256, 0, n, perm.p, c->d_px.p, c->d_py.p, c->d_pz.p, phi.p, plo.p);
@@ -1551,7 +1559,7 @@ int sort_points(inca_ctx* c, int64_t stride, int ppt, const double lo[3], double
       INCA_LAUNCH(c, k_boxes<5>, bb, 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p, boxes.p + 8 * nwt);
     else
       INCA_LAUNCH(c, k_boxes<4>, bb, 256, 0, tiles.p, nwt, phi.p, plo.p, boxes.p, boxes.p + 8 * nwt);
-    e = cudaStreamSynchronize(c->stream);  // the host tile table above is stack-owned
+    e = cudaGetLastError();
   }
   if (e) return cuda_error(c, e, "sorted grid");
   *n_out = n;
@@ -1566,25 +1574,19 @@ int prepare_sorted_grid(inca_ctx* c, bool sample, int ppt) {
   const bool sample_ok = !sample || (c->sample_version == c->grid_version && c->sample_stride_built == stride);
   if (main_ok && sample_ok) return INCA_OK;
   const int64_t n = c->ngrid;
-  // bounding box of the grid, reduced on the device (six values come back)
-  if (c->d_bbox.reserve(6)) return set_error(c, INCA_E_NOMEM, "bounding box");
+  // bounding box of the grid and the Morton key scale, reduced on the device and read there
+  if (c->d_bbox.reserve(7)) return set_error(c, INCA_E_NOMEM, "bounding box");
   INCA_LAUNCH(c, k_bbox, 1, 1024, 0, n, c->d_px.p, c->d_py.p, c->d_pz.p, c->d_bbox.p);
-  double bb[6];
-  INCA_CUDA(c, cudaMemcpyAsync(bb, c->d_bbox.p, sizeof(bb), cudaMemcpyDeviceToHost, c->stream));
-  INCA_CUDA(c, cudaStreamSynchronize(c->stream));
-  const double lo[3] = {bb[0], bb[1], bb[2]}, hi[3] = {bb[3], bb[4], bb[5]};
-  const double ext = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-12));
-  const double inv = 2097151.0 / ext;
   int64_t nn = 0;
   if (!main_ok) {
-    const int st = sort_points(c, 1, ppt, lo, inv, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
+    const int st = sort_points(c, 1, ppt, c->d_phi, c->d_plo, c->d_perm, c->d_wtbox, c->d_tiles, &nn,
                                &c->ntiles, c->mol_span);
     if (st) return st;
     c->mix_version = c->grid_version;
     c->mix_ppt = ppt;
   }
   if (!sample_ok) {
-    const int st = sort_points(c, stride, kSamplePPT, lo, inv, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
+    const int st = sort_points(c, stride, kSamplePPT, c->d_phi_s, c->d_plo_s, c->d_perm_s, c->d_wtbox_s,
                                c->d_tiles_s, &c->nsample, &c->ntiles_s, c->mol_span_s);
     if (st) return st;
     c->sample_version = c->grid_version;
@@ -2209,6 +2211,24 @@ int autotune_mixed(inca_ctx* c, double eps, int reps, int* ipc_out, int* stride_
       if (v != cur.slack && (st = consider({cur.ipc, cur.stride, cur.safety, cur.drop, cur.ctas, v, cur.ppt})))
         return st;
   }
+  // the estimate safety, the drop share and the cheap slack all spend the same error budget, so
+  // one at a time they stop at different optima from run to run: a joint sweep over each one's
+  // neighbours in its list (3 x 3 x 3 around the result) settles them together
+  auto near = [](const auto& list, auto v) {
+    const int n = static_cast<int>(sizeof(list) / sizeof(list[0]));
+    int i = 0;
+    while (i < n - 1 && list[i] != v) ++i;
+    return std::array<int, 2>{std::max(0, i - 1), std::min(n - 1, i + 1)};
+  };
+  const Sched base = cur;
+  const auto rs = near(safeties, base.safety), rd = near(drops, base.drop), rk = near(slacks, base.slack);
+  for (int a = rs[0]; a <= rs[1]; ++a)
+    for (int b = rd[0]; b <= rd[1]; ++b)
+      for (int k = rk[0]; k <= rk[1]; ++k) {
+        const Sched s{base.ipc, base.stride, safeties[a], drops[b], base.ctas, slacks[k], base.ppt};
+        if (s.safety == base.safety && s.drop == base.drop && s.slack == base.slack) continue;
+        if ((st = consider(s))) return st;
+      }
   apply(cur);
   *ipc_out = cur.ipc;
   *stride_out = cur.stride;

@@ -164,7 +164,8 @@ int inca_eval(inca_ctx* ctx, int mode, double tol, double* ivec);
  * 2^cheap_slack times the tile's drop threshold; that bound joins the left-out mass, which is
  * checked after the pass as before, so a large slack can cost a repeat, never accuracy).
  * inca_autotune times complete INCA_MIXED evaluations of the current grid and records (median
- * of reps each) over candidate schedules by coordinate descent, keeps the fastest in the
+ * of reps each) over candidate schedules by coordinate descent (two sweeps) and a joint sweep of
+ * estimate_safety, drop_fraction and cheap_slack around the result, keeps the fastest in the
  * context and reports it with the time of the default schedule; the last evaluation's results
  * stay on the device. inca_set_tuning sets a schedule (NULL: the defaults). Every schedule meets
  * the tolerance. No counterpart in the reference. */
