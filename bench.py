@@ -248,9 +248,9 @@ def batch_leg(ctx, device):
     to 200, symmetry-unique closed-shell DM2s) with at most 60 primitives -- a subset that fits
     one batch -- each as radial_plot s = 0..10 step 0.1 at nang 302 (nosym), thresh 1e-12, with
     records and grids resident: one batched preparation plus one replay of the captured
-    evaluation graph (mixed, 1e-8 per I(s)) and the I(s) reduction, against the molecules run one
-    after the other (preparation, plain FP64 evaluation, I(s)), each in its own context. Host
-    wall time around the (synchronous) calls."""
+    evaluation graph (mixed, 1e-8 per I(s), and again at 1e-10) and the I(s) reduction, against
+    the molecules run one after the other (preparation, plain FP64 evaluation, I(s)), each in its
+    own context. Host wall time around the (synchronous) calls."""
     from inca_parallel_gb300 import INCA_FP64, INCA_MIXED, Context, workloads as W
     scan = ([0.0], [10.0], [0.1], [302])
     mols = W.batch_workload(max_prims=60)
@@ -266,9 +266,9 @@ def batch_leg(ctx, device):
         ctx.batch_add_closed_shell(b["alpha"], b["tmn"], b["xyz"], D, *scan, unique=True, nosym=True)
     cnt = ctx.batch_prepare(THRESH)
 
-    def batched():
+    def batched(tol=TOL_SCAN):
         ctx.prepare(THRESH)
-        ctx.eval_graph(mode=INCA_MIXED, tol=TOL_SCAN, copy=False)
+        ctx.eval_graph(mode=INCA_MIXED, tol=tol, copy=False)
         return ctx.radial_plot()[1]
 
     def sequential(mode):
@@ -290,17 +290,21 @@ def batch_leg(ctx, device):
         return statistics.median(ts) * 1e3, out
 
     t_b, Ib = wall(batched, 5)  # the first call captures the graph; the timed ones replay it
+    t_b10, Ib10 = wall(lambda: batched(TOL_INTEGRAL), 5)  # the same at the radial integral's 1e-10
     t_64, (I64, qp) = wall(lambda: sequential(INCA_FP64), 2)
     t_mx, _ = wall(lambda: sequential(INCA_MIXED), 3)
     for c in ctxs:
         c.close()
     err = float(np.max(np.abs(Ib - I64) / np.abs(I64)))
+    err10 = float(np.max(np.abs(Ib10 - I64) / np.abs(I64)))
     return {"molecules": len(mols), "of_workload": 64, "primitives": [len(b["alpha"]) for _, b, _ in mols],
             "records": int(cnt[0]), "survivors": int(cnt[2]), "grid_points": int(ctx.ngrid),
             "quartet_points": int(qp), "batched_graph_ms": t_b, "batched_value": qp / (t_b * 1e-3),
             "sequential_fp64_ms": t_64, "sequential_mixed_ms": t_mx,
             "speedup_vs_sequential_fp64": t_64 / t_b, "speedup_vs_sequential_mixed": t_mx / t_b,
             "max_rel_err_I_s_vs_fp64": err, "tolerance_I_s": TOL_SCAN,
+            "at_tolerance_1e-10": {"batched_graph_ms": t_b10, "speedup_vs_sequential_fp64": t_64 / t_b10,
+                                   "max_rel_err_I_s_vs_fp64": err10},
             "note": "batched: one preparation of the whole batch and one graph replay of its mixed "
                     "evaluation; sequential: one context per molecule; preparation and I(s) on both sides"}
 
