@@ -37,6 +37,37 @@ def test_abi_version(lib):
     assert lib.inca_abi_version() == 2
 
 
+def test_struct_layouts_match_header(tmp_path):
+    # the ctypes mirrors of the header's structs: same fields at the same offsets, same size
+    # (compiled against include/inca_gpu.h with the host C compiler)
+    import ctypes
+    import shutil
+    import subprocess
+    from inca_parallel_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"inca_tuning": _lib.Tuning, "inca_counts": _lib.Counts}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "inca_gpu.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} . %zu\\n", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{name} {f} %zu\\n", offsetof({name}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        name, field, val = ln.split()
+        got[(name, field)] = int(val)
+    for name, cls in structs.items():
+        assert got[(name, ".")] == ctypes.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert got[(name, f)] == getattr(cls, f).offset, (name, f)
+
+
 def test_centercalc_matches_oracle(lib):
     import numpy as np
     import oracle_lib as O
