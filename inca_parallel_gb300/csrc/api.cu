@@ -98,6 +98,7 @@ int inca_ctx_destroy(inca_ctx* c) {
   c->d_pbad.release();
   c->d_pnruns.release();
   c->d_pn1.release();
+  c->d_pqrec.release();
   c->d_roff.release();
   c->d_rsum.release();
   c->d_classes.release();

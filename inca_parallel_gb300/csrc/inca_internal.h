@@ -151,6 +151,7 @@ struct inca_ctx {
   inca::DevBuf<unsigned char> d_ptmp;
   inca::DevBuf<int> d_pbad, d_pnruns;
   inca::DevBuf<unsigned long long> d_pn1;
+  inca::DevBuf<unsigned char> d_pqrec;  // each survivor's screened quartet, read by the record build
 
   // survivors, grouped by class
   int64_t nsurv = 0;

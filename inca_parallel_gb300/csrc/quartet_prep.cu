@@ -192,6 +192,11 @@ constexpr int kPairTableMax = 4096;
 // inca_prepare keeps its sort scratch (about 24 B per quartet plus the radix sort's temporary
 // storage) in the context for lists of up to 2^26 quartets (about 1.6 GB)
 constexpr int64_t kPrepKeepQuartets = int64_t(1) << 26;
+// Up to this many quartets the screening kernel keeps each survivor's quartet (QRec, 272 B: at
+// most 272 MiB) for the record build, which then reads it instead of repeating the FP64
+// normalisation, Gaussian products and Vandermonde solves (same values, so the same bits);
+// larger lists rebuild each survivor from its indices.
+constexpr int64_t kQRecCacheQuartets = int64_t(1) << 20;
 
 // One quartet (src/mod_intracule.f90:282-343). Returns 0 / 1 (screen 1) / 3 (both).
 // Jtab (optional): the JA8 table of k_pair_ja8.
@@ -259,17 +264,18 @@ __device__ __forceinline__ uint32_t class_key(const int L[3]) {
 
 __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl, const double* __restrict__ v,
                                        const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
-                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab);
+                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab,
+                                       QRec* qcache);
 
 // Pass 1: screening of every quartet; class key of survivors (others sort last).
 __global__ void k_screen(int64_t n, const int4* __restrict__ ijkl, const double* __restrict__ v,
                          const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
                          uint32_t* key, int64_t* idx, int* bad_index,
-                         unsigned long long* n_screen1, const double* __restrict__ Jtab) {
+                         unsigned long long* n_screen1, const double* __restrict__ Jtab, QRec* qcache) {
   const int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const bool live = q < n;
   int f = 0;
-  if (live) f = screen_one(q, ijkl, v, prims, flags, s1, s2, key, idx, bad_index, Jtab);
+  if (live) f = screen_one(q, ijkl, v, prims, flags, s1, s2, key, idx, bad_index, Jtab, qcache);
   // warp-aggregated count of screen-1 survivors
   const unsigned ballot = __ballot_sync(0xffffffffu, live && (f & 1));
   if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(n_screen1, static_cast<unsigned long long>(__popc(ballot)));
@@ -277,7 +283,8 @@ __global__ void k_screen(int64_t n, const int4* __restrict__ ijkl, const double*
 
 __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl, const double* __restrict__ v,
                                        const PrimD* __restrict__ prims, uint8_t* flags, double* s1, double* s2,
-                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab) {
+                                       uint32_t* key, int64_t* idx, int* bad_index, const double* Jtab,
+                                       QRec* qcache) {
   const int4 r = ijkl[q];
   idx[q] = q;
   if (r.x < 1 || r.y < 1 || r.z < 1 || r.w < 1 || r.x > cP.nprim || r.y > cP.nprim ||
@@ -293,6 +300,7 @@ __device__ __noinline__ int screen_one(int64_t q, const int4* __restrict__ ijkl,
   double a1, a2;
   const int f = prepare_one(prims, r, v[q], &rec, &a1, &a2, Jtab);
   flags[q] = static_cast<uint8_t>(f);
+  if (qcache && f == 3) qcache[q] = rec;
   if (s1) s1[q] = a1;
   if (s2) s2[q] = a2;
   // sort key: molecule (batches), then angular class; quartets that fail screening sort last
@@ -312,7 +320,7 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
                         const int4* __restrict__ ijkl, const double* __restrict__ v,
                         const PrimD* __restrict__ prims, const ClassSeg* __restrict__ segs,
                         int nseg, double* rec64, float* rec32, int64_t* surv_src,
-                        const double* __restrict__ Jtab) {
+                        const double* __restrict__ Jtab, const QRec* __restrict__ qcache) {
   const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (p >= nsurv) return;
   int lo = 0, hi = nseg - 1;
@@ -324,8 +332,12 @@ __global__ void k_build(int64_t nsurv, const int64_t* __restrict__ sorted_idx,
   const int64_t src = sorted_idx[p];
   surv_src[p] = src;
   QRec rec;
-  double a1, a2;
-  prepare_one(prims, ijkl[src], v[src], &rec, &a1, &a2, Jtab);
+  if (qcache) {
+    rec = qcache[src];
+  } else {
+    double a1, a2;
+    prepare_one(prims, ijkl[src], v[src], &rec, &a1, &a2, Jtab);
+  }
   const int64_t local = p - sg.first;
   double* r64 = rec64 + sg.off64 + local * sg.stride;
   // u-space polynomials: V_d(r') = sum_k C_k r'^k = sum_k (C_k c^-k) u^k, u = c r'
@@ -453,9 +465,10 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   DevBuf<uint32_t>& ukeys = c->d_pukeys;
   DevBuf<int64_t>& ucounts = c->d_pucounts;
   DevBuf<int>& nruns = c->d_pnruns;
+  DevBuf<unsigned char>& qrec = c->d_pqrec;
   auto release_all = [&]() {
     key.release(); key2.release(); idx.release(); idx2.release(); bad.release(); n1dev.release();
-    tmp.release(); ukeys.release(); ucounts.release(); nruns.release();
+    tmp.release(); ukeys.release(); ucounts.release(); nruns.release(); qrec.release();
   };
   const bool keep_scratch = n <= kPrepKeepQuartets;
   auto cleanup = [&]() {
@@ -464,6 +477,13 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   if (key.reserve(n) || key2.reserve(n) || idx.reserve(n) || idx2.reserve(n) || bad.reserve(1) || n1dev.reserve(1)) {
     release_all();
     return set_error(c, INCA_E_NOMEM, "inca_prepare: sort buffers");
+  }
+  QRec* qcache = nullptr;
+  if (n <= kQRecCacheQuartets) {
+    if (qrec.reserve(sizeof(QRec) * std::max<int64_t>(n, 1)) == cudaSuccess)
+      qcache = reinterpret_cast<QRec*>(qrec.p);
+    else
+      (void)cudaGetLastError();  // no room: build the records from the indices instead
   }
   cudaError_t e = cudaMemsetAsync(bad.p, 0, sizeof(int), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(n1dev.p, 0, sizeof(unsigned long long), c->stream);
@@ -485,7 +505,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
     INCA_LAUNCH(c, k_screen, static_cast<unsigned>(grid), bs, 0, n, c->d_ijkl.p, c->d_v.p, c->d_prims.p, c->d_flags.p,
                                                                 keep_values ? c->d_s1.p : nullptr,
                                                                 keep_values ? c->d_s2.p : nullptr, key.p, idx.p, bad.p,
-                                                                n1dev.p, jtab);
+                                                                n1dev.p, jtab, qcache);
     e = cudaGetLastError();
   }
   size_t tmp_bytes = 0;
@@ -596,7 +616,7 @@ int prepare_device(inca_ctx* c, double thresh, int normalize) {
   if (e == cudaSuccess && nsurv > 0) {
     INCA_LAUNCH(c, k_build, static_cast<unsigned>((nsurv + bs - 1) / bs), bs, 0, 
         nsurv, idx2.p, c->d_ijkl.p, c->d_v.p, c->d_prims.p, c->d_classes.p,
-        static_cast<int>(c->classes.size()), c->d_rec64.p, c->d_rec32.p, c->d_surv_src.p, jtab);
+        static_cast<int>(c->classes.size()), c->d_rec64.p, c->d_rec32.p, c->d_surv_src.p, jtab, qcache);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
