@@ -11,8 +11,9 @@
 //
 // Work layout. Points are evaluated in Morton order (a sorted copy of the grid). A CTA is one
 // warp owning a tile of 32 kPPT consecutive points (kPPT = 3, 4 or 5 per lane, set by the
-// schedule; 32-point sub-tiles p = lane + 32 k), each a compact region with a bounding box. The CTA walks a strided subset of the class-uniform
-// chunks (<= 32 quartet records of one angular class); each chunk is staged into shared memory
+// schedule; 32-point sub-tiles p = lane + 32 k), each a compact region with a bounding box. The
+// CTA walks a strided subset of the class-uniform chunks (<= 32 quartet records of one angular
+// class); each chunk is staged into shared memory
 // by a 1-D TMA bulk copy (cp.async.bulk + mbarrier), double-buffered so the next chunk's copy
 // overlaps the current chunk's arithmetic. All waits are bounded; a wait that gives up sets an
 // error word that the host turns into INCA_E_TIMEOUT.
